@@ -1,0 +1,196 @@
+/*
+ * sdt_gb300.h -- C ABI of libsdt_gb300.so, a GB300 (sm_103a) implementation
+ * of NWChem's TCE CCSD(T) perturbative-triples tile path.
+ *
+ * Two surfaces are exported.
+ *
+ *  1. The tile-level surface the reference's CUDA (T) driver binds
+ *     (src/tce/ccsd_t/ccsd_t_gpu.F, ccsd_t_singles_gpu.F,
+ *     ccsd_t_doubles_gpu.F).  Same Fortran-mangled names, same argument
+ *     order, 64-bit Integer passed by reference (the reference is built -i8,
+ *     src/tce/ccsd_t/header.h:51), same accumulate-into-device-tile
+ *     semantics.  Sub-blocks come from host memory and are copied per call.
+ *
+ *  2. A batched surface (sdt_*) that replaces the whole ccsd_t(...) call
+ *     (src/tce/ccsd_t/ccsd_t.F:19-20): the T1/T2/V2 TCE files (hash table +
+ *     block data) go to the device once, and one fused kernel evaluates all
+ *     27 tile kernels and the energy sum for every tuple.
+ *
+ * No torch types appear here.  Streams are passed as void* (cudaStream_t);
+ * NULL means the library's own stream.
+ */
+#ifndef SDT_GB300_H
+#define SDT_GB300_H
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int64_t sdt_int; /* Fortran Integer (-i8) */
+
+/* ------------------------------------------------------------------------
+ * 1. Reference tile-level ABI (sd_t_total.cu, memory.cu, hybrid.c)
+ * --------------------------------------------------------------------- */
+
+/* s1: t3_s[perm_k] +/-= t1sub(p4,h1) * v2sub(h3,h2,p6,p5).
+ * Replaces sd_t_s1_k_cuda_ (sd_t_total.cu:5522-5526 for k=1; the other k
+ * follow it in that file).  The t3 argument is ignored, as in the reference:
+ * the singles tile lives on the device (dev_mem_s_). */
+#define SDT_S1_DECL(k)                                                       \
+    void sd_t_s1_##k##_cuda_(sdt_int *h1d, sdt_int *h2d, sdt_int *h3d,       \
+                             sdt_int *p4d, sdt_int *p5d, sdt_int *p6d,       \
+                             double *t3, double *t1sub, double *v2sub);
+SDT_S1_DECL(1) SDT_S1_DECL(2) SDT_S1_DECL(3) SDT_S1_DECL(4) SDT_S1_DECL(5)
+SDT_S1_DECL(6) SDT_S1_DECL(7) SDT_S1_DECL(8) SDT_S1_DECL(9)
+
+/* d1: t3[perm_k] -/+= sum_h7 t2sub(h7,p4,p5,h1) * v2sub(h3,h2,p6,h7).
+ * Replaces sd_t_d1_k_cuda_ (sd_t_total.cu:312-316 for k=1). */
+#define SDT_D1_DECL(k)                                                       \
+    void sd_t_d1_##k##_cuda_(sdt_int *h1d, sdt_int *h2d, sdt_int *h3d,       \
+                             sdt_int *h7d, sdt_int *p4d, sdt_int *p5d,       \
+                             sdt_int *p6d, double *t3, double *t2sub,        \
+                             double *v2sub);
+SDT_D1_DECL(1) SDT_D1_DECL(2) SDT_D1_DECL(3) SDT_D1_DECL(4) SDT_D1_DECL(5)
+SDT_D1_DECL(6) SDT_D1_DECL(7) SDT_D1_DECL(8) SDT_D1_DECL(9)
+
+/* d2: t3[perm_k] -/+= sum_p7 t2sub(p7,p4,h1,h2) * v2sub(p7,h3,p6,p5).
+ * Replaces sd_t_d2_k_cuda_ (sd_t_total.cu:2885-2888 for k=1). */
+#define SDT_D2_DECL(k)                                                       \
+    void sd_t_d2_##k##_cuda_(sdt_int *h1d, sdt_int *h2d, sdt_int *h3d,       \
+                             sdt_int *p4d, sdt_int *p5d, sdt_int *p6d,       \
+                             sdt_int *p7d, double *t3, double *t2sub,        \
+                             double *v2sub);
+SDT_D2_DECL(1) SDT_D2_DECL(2) SDT_D2_DECL(3) SDT_D2_DECL(4) SDT_D2_DECL(5)
+SDT_D2_DECL(6) SDT_D2_DECL(7) SDT_D2_DECL(8) SDT_D2_DECL(9)
+
+/* Energy of the current device tiles: energy[0] is set (not added) to
+ * E[T] = factor*sum t3^2/D and energy[1] to
+ * E(T) = factor*sum t3*(t3+t3_s)/D, D = e_h1+e_h2+e_h3-e_p4-e_p5-e_p6.
+ * host1/host2 are ignored, as in the reference.
+ * Replaces compute_en_ (sd_t_total.cu:5373-5379). */
+void compute_en_(double *factor, double *energy, double *eval1,
+                 double *eval2, double *eval3, double *eval4, double *eval5,
+                 double *eval6, sdt_int *h1d, sdt_int *h2d, sdt_int *h3d,
+                 sdt_int *p4d, sdt_int *p5d, sdt_int *p6d, double *host1,
+                 double *host2);
+
+/* Allocate and zero the doubles / singles triples tiles of one tuple
+ * (tuple dims).  Replace dev_mem_d_ (sd_t_total.cu:12-16) and dev_mem_s_
+ * (sd_t_total.cu:5392-5396). */
+void dev_mem_d_(sdt_int *h1d, sdt_int *h2d, sdt_int *h3d, sdt_int *p4d,
+                sdt_int *p5d, sdt_int *p6d);
+void dev_mem_s_(sdt_int *h1d, sdt_int *h2d, sdt_int *h3d, sdt_int *p4d,
+                sdt_int *p5d, sdt_int *p6d);
+/* Release both tiles (sd_t_total.cu:17-28). */
+void dev_release_(void);
+/* Caching device / pinned-host allocator (memory.cu:69,164-178).  Blocks
+ * freed between init and finalize are reused by size; finalize checks that
+ * nothing is live. */
+void initmemmodule_(void);
+void finalizememmodule_(void);
+/* Device binding (hybrid.c:25,32): check_device_ returns 1 when this
+ * process's device index (SDT_LOCAL_RANK / LOCAL_RANK, default 0) is below
+ * *icuda; device_init_ selects that device, or sets *cuda_device_number =
+ * 30 when fewer than *icuda devices exist (the reference's warning path). */
+int check_device_(long *icuda);
+int device_init_(long *icuda, long *cuda_device_number);
+
+/* ------------------------------------------------------------------------
+ * Error handling.  The reference prints and exit(1)s on any CUDA error
+ * (header.h:28-36).  The Fortran-facing symbols above keep that behaviour
+ * by default (SDT_ERRMODE_EXIT); SDT_ERRMODE_RECORD makes them record the
+ * error instead, readable with sdt_last_error().  The sdt_* functions
+ * always return a status and never exit.
+ * --------------------------------------------------------------------- */
+enum {
+    SDT_OK = 0,
+    SDT_ERR_ARG = 1,      /* bad argument or size                        */
+    SDT_ERR_CUDA = 2,     /* CUDA runtime error                          */
+    SDT_ERR_NOMEM = 3,    /* allocation failed                           */
+    SDT_ERR_STATE = 4,    /* call out of order (e.g. no dev_mem_d_)      */
+    SDT_ERR_MISSING = 5,  /* a block the path needs is absent            */
+    SDT_ERR_TIMEOUT = 6   /* a bounded device wait ran out               */
+};
+enum { SDT_ERRMODE_EXIT = 0, SDT_ERRMODE_RECORD = 1 };
+void sdt_set_error_mode(int mode);
+int sdt_last_error(char *msg, size_t len); /* returns code, clears it */
+
+/* ------------------------------------------------------------------------
+ * 2. Batched surface
+ * --------------------------------------------------------------------- */
+
+/* Tile description; arrays indexed by tile-1, tiles 1..noab occupied and
+ * noab+1..noab+nvab virtual (src/tce/include/tce.fh:14-21). */
+typedef struct {
+    int64_t noab, nvab;
+    const int64_t *range;
+    const int64_t *spin;
+    const int64_t *sym;
+    const int64_t *offset;     /* into evl_sorted */
+    const int64_t *alpha;      /* beta->alpha tile map; NULL if unrestricted */
+    const double *evl_sorted;  /* orbital energies, occupied then virtual */
+    int64_t restricted;
+} sdt_tiling;
+
+/* A TCE file: hash in the tce_hash layout (hash[0] = n, keys ascending in
+ * hash[1..n], block offsets in hash[n+1..2n]) and ndata doubles of blocks. */
+typedef struct {
+    const int64_t *hash;
+    const double *data;
+    int64_t ndata;
+} sdt_file;
+
+/* Tuple list of the (T) driver (ccsd_t_6tasks / ccsd_t_neword,
+ * src/tce/ccsd_t/ccsd_t_neword.F:1-217).  klist gets 7*n entries
+ * (p4b,p5b,p6b,h1b,h2b,h3b,weight), weight-ordered like the reference. */
+int64_t sdt_tasks_count(const sdt_tiling *t);
+int sdt_tasks_list(const sdt_tiling *t, int64_t n, int64_t *klist);
+/* Algorithmic FLOPs of the listed tuples: sum Nt*18*(O_allowed+V_allowed+1). */
+double sdt_tasks_flops(const sdt_tiling *t, const int64_t *klist, int64_t n);
+
+/* Synthetic seeded TCE files (the inputs the path reads).  kind: 0 = T1,
+ * 1 = T2, 2 = V2 (vvov, ovoo and vvoo blocks in one hash).  Query sizes
+ * with hash == data == NULL, then fill. */
+enum { SDT_FILE_T1 = 0, SDT_FILE_T2 = 1, SDT_FILE_V2 = 2 };
+int sdt_synth_file(const sdt_tiling *t, int kind, uint64_t seed,
+                   int64_t *nblocks, int64_t *ndata, int64_t *hash,
+                   double *data);
+/* Orbital energies: occupied ~ U[-1.5,-0.4], virtual ~ U[0.2,2.5]. */
+int sdt_synth_evl(int64_t nocc, int64_t nvir, uint64_t seed, double *evl);
+
+/* A job holds one (T) problem resident on the device. */
+typedef struct sdt_job sdt_job;
+enum { SDT_PREC_FP64 = 0 };
+int sdt_job_create(const sdt_tiling *t, sdt_job **job);
+/* Copy the host TCE files to the device and re-lay them out for the fused
+ * kernel (antisymmetric mirrors, signs of tce_hashnsort.F).  Device-side
+ * copies are enqueued on stream; the call returns after the host buffers
+ * may be reused. */
+int sdt_job_load(sdt_job *job, const sdt_file *t1, const sdt_file *t2,
+                 const sdt_file *v2, void *stream);
+/* Evaluate the tuples klist[0..n-1] (7 entries each).  energy[0] = E[T],
+ * energy[1] = E(T).  per_task (optional, 2*n doubles, host) receives each
+ * tuple's pair.  Synchronises the stream. */
+int sdt_job_run(sdt_job *job, const int64_t *klist, int64_t n,
+                int precision, double *energy, double *per_task,
+                void *stream);
+int sdt_job_destroy(sdt_job *job);
+/* Device bytes held by a job. */
+int64_t sdt_job_device_bytes(const sdt_job *job);
+
+/* One-shot replacement for ccsd_t(d_t1,k_t1_offset,d_t2,k_t2_offset,
+ * d_v2,k_v2_offset,energy1,energy2,size_t1) (ccsd_t.F:19-20): builds the
+ * tuple list, loads the files, runs every tuple and returns E[T] in
+ * *energy1 and E(T) in *energy2. */
+int sdt_ccsd_t(const sdt_tiling *t, const sdt_file *t1, const sdt_file *t2,
+               const sdt_file *v2, double *energy1, double *energy2);
+
+/* Kernel launches made by this library since load (all entry points). */
+int64_t sdt_launch_count(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,819 @@
+// sdt_fused.cu -- batched (T): device ingest of the TCE files and the fused
+// FP64 tuple kernel.
+//
+// The reference evaluates one tuple (p4b<=p5b<=p6b, h1b<=h2b<=h3b) as 9 s1,
+// 9 d1 (per h7b) and 9 d2 (per p7b) kernel calls into two Nt-sized device
+// tiles, then a separate energy kernel (src/tce/ccsd_t/ccsd_t_gpu.F:87-241,
+// sd_t_total.cu).  Here one CTA owns a 4x4x4x4x4x4 sub-box of one tuple's
+// triples tile.  It accumulates all 18 d1/d2 contractions into that sub-box
+// in shared memory with FP64 tensor-core MMAs (mma.sync m8n8k4.f64), adds
+// the 9 s1 products and the orbital-energy denominator in the epilogue and
+// writes one (E[T], E(T)) pair.  The triples tile never reaches HBM.
+//
+// In tuple coordinates (a,b,c in tiles p4b,p5b,p6b; i,j,k in h1b,h2b,h3b;
+// t = T2, w = <h7 p6||h2 h3>, v = <p5 p6||h3 p7>, u = <p5 p6||h2 h3>, and
+// t(p,q;h,l) read with the antisymmetry signs of tce_hashnsort.F) the
+// 27 reference kernels (ccsd_t_kernels_omp.F) add up to:
+//   d1:  -t(ab;im)w(mcjk) +t(ab;jm)w(mcik) -t(ab;km)w(mcij)
+//        -t(bc;im)w(majk) +t(bc;jm)w(maik) -t(bc;km)w(maij)
+//        +t(ac;im)w(mbjk) -t(ac;jm)w(mbik) +t(ac;km)w(mbij)     (sum over m)
+//   d2:  -t(ae;ij)v(bcke) -t(ae;jk)v(bcie) +t(ae;ik)v(bcje)
+//        +t(be;ij)v(acke) +t(be;jk)v(acie) -t(be;ik)v(acje)
+//        -t(ce;ij)v(abke) -t(ce;jk)v(abie) +t(ce;ik)v(abje)     (sum over e)
+//   s1:  +t1(ai)u(bcjk) -t1(aj)u(bcik) +t1(ak)u(bcij)
+//        -t1(bi)u(acjk) +t1(bj)u(acik) -t1(bk)u(acij)
+//        +t1(ci)u(abjk) -t1(cj)u(abik) +t1(ck)u(abij)
+// (row k of each block is kernel k of its family, in order).
+#include "sdt_common.cuh"
+
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
+namespace sdt {
+namespace {
+
+// ---------------------------------------------------------------------------
+// Dense device layouts (global orbital indices within each space):
+//   T1d[a][i]                      v x o
+//   T2a[p][q][h][l]                v x v x o x o   (d1 operand, l = summed m)
+//   T2b[p][h][l][q]                v x o x o x v   (d2 operand, q = summed e)
+//   Wd1[c][j][k][m]                v x o x o x o   (<m c||j k>, m fastest)
+//   Vd2 per virtual tile pair B<=C: [b][c][k][e] with b,c tile-local
+//   Ud[b][c][j][k]                 v x v x o x o   (<b c||j k>)
+// Entries the path never reads (non-canonical orders of V2) stay zero, as
+// do blocks that spin or irrep forbid.
+// ---------------------------------------------------------------------------
+struct CopyJob {
+    int64_t src;          // offset of the 3-D slab in the raw file
+    int64_t dst;          // element offset in the destination array
+    int64_t n1, n2, n3;   // slab dims (key order, last fastest)
+    int64_t s1, s2, s3;   // destination strides of those dims
+    double sign;
+    int32_t src_file;     // 0 T1, 1 T2, 2 V2
+    int32_t dst_array;    // index into the destination table
+};
+
+enum { DST_T1 = 0, DST_T2A, DST_T2B, DST_VD2, DST_WD1, DST_UD, DST_N };
+
+struct IngestArgs {
+    const double *src[3];
+    double *dst[DST_N];
+    const CopyJob *jobs;
+};
+
+__global__ void __launch_bounds__(256) ingest_kernel(const IngestArgs g) {
+    const CopyJob j = g.jobs[blockIdx.x];
+    const double *__restrict__ s = g.src[j.src_file] + j.src;
+    double *__restrict__ d = g.dst[j.dst_array] + j.dst;
+    const int64_t n = j.n1 * j.n2 * j.n3;
+    for (int64_t e = threadIdx.x; e < n; e += blockDim.x) {
+        const int64_t x3 = e % j.n3, t = e / j.n3;
+        const int64_t x2 = t % j.n2, x1 = t / j.n2;
+        d[x1 * j.s1 + x2 * j.s2 + x3 * j.s3] = j.sign * s[e];
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Fused tuple kernel.
+// ---------------------------------------------------------------------------
+constexpr int BOX = 4;          // sub-box edge in every index
+constexpr int NX = 4096;        // BOX^6
+constexpr int kThreads = 128;   // 4 warps, 2x2 over the 64x64 term GEMM
+constexpr int kMaxTiles = 256;
+
+// Term table: row dims (r) and column dims (c) of the 64x64 GEMM, sign.
+// Dims: 0=a 1=b 2=c 3=i 4=j 5=k.
+struct TermDef {
+    int8_t r[3], c[3];
+    int8_t sign;
+};
+// d1: rows (P,P',H) of t(P,P';H,m); cols (Q,H',H'') of w(m,Q,H',H'').
+__constant__ TermDef kD1[9] = {
+    {{0, 1, 3}, {2, 4, 5}, -1}, {{0, 1, 4}, {2, 3, 5}, +1}, {{0, 1, 5}, {2, 3, 4}, -1},
+    {{1, 2, 3}, {0, 4, 5}, -1}, {{1, 2, 4}, {0, 3, 5}, +1}, {{1, 2, 5}, {0, 3, 4}, -1},
+    {{0, 2, 3}, {1, 4, 5}, +1}, {{0, 2, 4}, {1, 3, 5}, -1}, {{0, 2, 5}, {1, 3, 4}, +1}};
+// d2: rows (P,H,H') of t(P,e;H,H'); cols (Q,Q',H'') of v(Q,Q',H'',e).
+__constant__ TermDef kD2[9] = {
+    {{0, 3, 4}, {1, 2, 5}, -1}, {{0, 4, 5}, {1, 2, 3}, -1}, {{0, 3, 5}, {1, 2, 4}, +1},
+    {{1, 3, 4}, {0, 2, 5}, +1}, {{1, 4, 5}, {0, 2, 3}, +1}, {{1, 3, 5}, {0, 2, 4}, -1},
+    {{2, 3, 4}, {0, 1, 5}, -1}, {{2, 4, 5}, {0, 1, 3}, -1}, {{2, 3, 5}, {0, 1, 4}, +1}};
+
+struct FusedParams {
+    const double *T1d, *T2a, *T2b, *Vd2, *Wd1, *Ud;
+    const int64_t *pair_off;  // [nvab*nvab], virtual tile pair -> Vd2 region
+    const double *evl;        // occupied then virtual
+    const int32_t *tiles;     // [ntiles][4] = start in space, range, spin, sym
+    int32_t noab, nvab;
+    int64_t nocc, nvir;
+    const int64_t *klist;     // [n][7]
+    const int64_t *item_pref; // [n+1]
+    const double *factor;     // [n]
+    int64_t n_tasks, item_base;
+    double *part;             // [items][2]
+};
+
+struct TupleCtx {
+    int32_t tile[6];
+    int32_t ext[6];
+    int32_t start[6];
+    int32_t boff[6];
+};
+
+__device__ __forceinline__ int stride6(int d) { return 1 << (2 * (5 - d)); }
+
+// One d1 (kind 1) or d2 (kind 2) term accumulated into X.
+__device__ __forceinline__ void run_term(const FusedParams &p, const TupleCtx &t,
+                                      const int32_t (*__restrict__ st)[4],
+                                      double *__restrict__ X, int kind, int term) {
+    const TermDef td = kind == 1 ? kD1[term] : kD2[term];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int r = lane >> 2, q = lane & 3;
+    const int wm = warp >> 1, wn = warp & 1;
+
+    int64_t abase[4], bbase[4];
+    unsigned aok = 0, bok = 0;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        const int m = wm * 32 + i * 8 + r;
+        const int l0 = m >> 4, l1 = (m >> 2) & 3, l2 = m & 3;
+        const int x0 = t.boff[td.r[0]] + l0, x1 = t.boff[td.r[1]] + l1, x2 = t.boff[td.r[2]] + l2;
+        const bool ok = x0 < t.ext[td.r[0]] && x1 < t.ext[td.r[1]] && x2 < t.ext[td.r[2]];
+        aok |= ok ? (1u << i) : 0u;
+        const int64_t g0 = t.start[td.r[0]] + x0, g1 = t.start[td.r[1]] + x1,
+                      g2 = t.start[td.r[2]] + x2;
+        abase[i] = ok ? (kind == 1 ? ((g0 * p.nvir + g1) * p.nocc + g2) * p.nocc
+                                   : ((g0 * p.nocc + g1) * p.nocc + g2) * p.nvir)
+                      : 0;
+    }
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        const int n = wn * 32 + j * 8 + r;
+        const int l0 = n >> 4, l1 = (n >> 2) & 3, l2 = n & 3;
+        const int x0 = t.boff[td.c[0]] + l0, x1 = t.boff[td.c[1]] + l1, x2 = t.boff[td.c[2]] + l2;
+        const bool ok = x0 < t.ext[td.c[0]] && x1 < t.ext[td.c[1]] && x2 < t.ext[td.c[2]];
+        bok |= ok ? (1u << j) : 0u;
+        const int64_t g0 = t.start[td.c[0]] + x0, g2 = t.start[td.c[2]] + x2;
+        int64_t b;
+        if (kind == 1) {
+            const int64_t g1 = t.start[td.c[1]] + x1;
+            b = ((g0 * p.nocc + g1) * p.nocc + g2) * p.nocc;
+        } else {
+            const int64_t pr = (int64_t)(t.tile[td.c[0]] - p.noab - 1) * p.nvab +
+                               (t.tile[td.c[1]] - p.noab - 1);
+            b = p.pair_off[pr] + (((int64_t)x0 * t.ext[td.c[1]] + x1) * p.nocc + g2) * p.nvir;
+        }
+        bbase[j] = ok ? b : 0;
+    }
+
+    double acc[4][4][2];
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc[i][j][0] = acc[i][j][1] = 0.0;
+
+    const double *__restrict__ A = kind == 1 ? p.T2a : p.T2b;
+    const double *__restrict__ B = kind == 1 ? p.Wd1 : p.Vd2;
+    // Allowed summed tiles: the T2 quad read must balance spin and irrep
+    // (tce_hashnsort.F:31-36 for d1, :107-111 for d2).
+    const int tP = t.tile[td.r[0]], tX = t.tile[td.r[1]], tY = t.tile[td.r[2]];
+    const int sP = st[tP - 1][2], sX = st[tX - 1][2], sY = st[tY - 1][2];
+    const int yP = st[tP - 1][3], yX = st[tX - 1][3], yY = st[tY - 1][3];
+    const int first = kind == 1 ? 1 : p.noab + 1;
+    const int last = kind == 1 ? p.noab : p.noab + p.nvab;
+    int kt = first;
+    while (kt <= last) {
+        // Merge a run of consecutive allowed tiles into one K range.
+        auto allowed = [&](int e) {
+            const int se = st[e - 1][2], ye = st[e - 1][3];
+            return kind == 1 ? (sP + sX == sY + se && (yP ^ yX ^ yY ^ ye) == 0)
+                             : (sP + se == sX + sY && (yP ^ ye ^ yX ^ yY) == 0);
+        };
+        if (!allowed(kt)) {
+            ++kt;
+            continue;
+        }
+        const int64_t k_begin = st[kt - 1][0];
+        int64_t k_end = k_begin + st[kt - 1][1];
+        ++kt;
+        while (kt <= last && allowed(kt)) {
+            k_end += st[kt - 1][1];
+            ++kt;
+        }
+        for (int64_t k0 = k_begin; k0 < k_end; k0 += 4) {
+            const int64_t k = k0 + q;
+            const bool kok = k < k_end;
+            double a[4], b[4];
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                a[i] = (kok && (aok >> i & 1u)) ? __ldg(A + abase[i] + k) : 0.0;
+                b[i] = (kok && (bok >> i & 1u)) ? __ldg(B + bbase[i] + k) : 0.0;
+            }
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+#pragma unroll
+                for (int j = 0; j < 4; ++j) dmma_8x8x4(acc[i][j][0], acc[i][j][1], a[i], b[j]);
+        }
+    }
+
+    // Scatter the 64x64 result into the sub-box (a bijection, no conflicts).
+    const double sign = (double)td.sign;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        if (!(aok >> i & 1u)) continue;
+        const int m = wm * 32 + i * 8 + r;
+        const int roff = (m >> 4) * stride6(td.r[0]) + ((m >> 2) & 3) * stride6(td.r[1]) +
+                         (m & 3) * stride6(td.r[2]);
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                const int n = wn * 32 + j * 8 + 2 * q + h;
+                const int l0 = n >> 4, l1 = (n >> 2) & 3, l2 = n & 3;
+                if (t.boff[td.c[0]] + l0 >= t.ext[td.c[0]] || t.boff[td.c[1]] + l1 >= t.ext[td.c[1]] ||
+                    t.boff[td.c[2]] + l2 >= t.ext[td.c[2]])
+                    continue;
+                const int off = roff + l0 * stride6(td.c[0]) + l1 * stride6(td.c[1]) +
+                                l2 * stride6(td.c[2]);
+                X[off] += sign * acc[i][j][h];
+            }
+    }
+    __syncthreads();
+}
+
+__global__ void __launch_bounds__(kThreads, 4) fused_fp64_kernel(const FusedParams p) {
+    __shared__ double X[NX];
+    __shared__ int32_t st[kMaxTiles][4];
+    __shared__ double red[2][kThreads / 32];
+
+    const int64_t item = p.item_base + blockIdx.x;
+    // Tuple owning this item: last q with item_pref[q] <= item.
+    int64_t lo = 0, hi = p.n_tasks - 1;
+    while (lo < hi) {
+        const int64_t mid = (lo + hi + 1) >> 1;
+        if (p.item_pref[mid] <= item) lo = mid;
+        else hi = mid - 1;
+    }
+    const int64_t tq = lo;
+    int64_t local = item - p.item_pref[tq];
+
+    const int ntiles = p.noab + p.nvab;
+    for (int e = threadIdx.x; e < ntiles * 4; e += kThreads) st[e >> 2][e & 3] = p.tiles[e];
+    for (int e = threadIdx.x; e < NX; e += kThreads) X[e] = 0.0;
+    __syncthreads();
+
+    TupleCtx t;
+#pragma unroll
+    for (int d = 0; d < 6; ++d) {
+        t.tile[d] = (int32_t)p.klist[7 * tq + d];
+        t.ext[d] = st[t.tile[d] - 1][1];
+        t.start[d] = st[t.tile[d] - 1][0];
+    }
+#pragma unroll
+    for (int d = 5; d >= 0; --d) {
+        const int nb = (t.ext[d] + BOX - 1) / BOX;
+        t.boff[d] = (int32_t)(local % nb) * BOX;
+        local /= nb;
+    }
+
+#pragma unroll 1
+    for (int term = 0; term < 18; ++term) run_term(p, t, st, X, term < 9 ? 1 : 2, term % 9);
+
+    // Epilogue: s1 terms, denominator and the (E[T], E(T)) sums in FP64
+    // (ccsd_t_dot.F:101-124).
+    const double factor = p.factor[tq];
+    const double *__restrict__ eo = p.evl;
+    const double *__restrict__ ev = p.evl + p.nocc;
+    const int64_t v = p.nvir, o = p.nocc;
+    double s1 = 0.0, s2 = 0.0;
+    for (int e = threadIdx.x; e < NX; e += kThreads) {
+        int l[6];
+#pragma unroll
+        for (int d = 0; d < 6; ++d) l[d] = (e >> (2 * (5 - d))) & 3;
+        bool ok = true;
+#pragma unroll
+        for (int d = 0; d < 6; ++d) ok = ok && (t.boff[d] + l[d] < t.ext[d]);
+        if (!ok) continue;
+        const int64_t a = t.start[0] + t.boff[0] + l[0], b = t.start[1] + t.boff[1] + l[1],
+                      c = t.start[2] + t.boff[2] + l[2], i = t.start[3] + t.boff[3] + l[3],
+                      j = t.start[4] + t.boff[4] + l[4], k = t.start[5] + t.boff[5] + l[5];
+        const double *T1 = p.T1d, *U = p.Ud;
+        auto u = [&](int64_t x, int64_t y, int64_t h, int64_t g) {
+            return __ldg(U + ((x * v + y) * o + h) * o + g);
+        };
+        auto t1 = [&](int64_t x, int64_t h) { return __ldg(T1 + x * o + h); };
+        double sing = t1(a, i) * u(b, c, j, k);
+        sing -= t1(a, j) * u(b, c, i, k);
+        sing += t1(a, k) * u(b, c, i, j);
+        sing -= t1(b, i) * u(a, c, j, k);
+        sing += t1(b, j) * u(a, c, i, k);
+        sing -= t1(b, k) * u(a, c, i, j);
+        sing += t1(c, i) * u(a, b, j, k);
+        sing -= t1(c, j) * u(a, b, i, k);
+        sing += t1(c, k) * u(a, b, i, j);
+        const double doub = X[e];
+        const double denom_0 = -(ev[a] + ev[b] + ev[c]);
+        const double denom = doub * factor / (eo[i] + eo[j] + eo[k] + denom_0);
+        s1 += denom * doub;
+        s2 += denom * (doub + sing);
+    }
+    s1 = warp_sum(s1);
+    s2 = warp_sum(s2);
+    if ((threadIdx.x & 31) == 0) {
+        red[0][threadIdx.x >> 5] = s1;
+        red[1][threadIdx.x >> 5] = s2;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double x = 0.0, y = 0.0;
+        for (int w = 0; w < kThreads / 32; ++w) {
+            x += red[0][w];
+            y += red[1][w];
+        }
+        p.part[2 * item] = x;
+        p.part[2 * item + 1] = y;
+    }
+}
+
+// Per-tuple sums of item partials (fixed order, compensated).
+__global__ void __launch_bounds__(256) tuple_sum_kernel(const double *__restrict__ part,
+                                                        const int64_t *__restrict__ pref,
+                                                        int64_t n, double *__restrict__ out) {
+    const int64_t q = blockIdx.x;
+    if (q >= n) return;
+    __shared__ double sa[256], ca[256], sb[256], cb[256];
+    Comp x, y;
+    for (int64_t it = pref[q] + threadIdx.x; it < pref[q + 1]; it += 256) {
+        x.add(part[2 * it]);
+        y.add(part[2 * it + 1]);
+    }
+    sa[threadIdx.x] = x.s;
+    ca[threadIdx.x] = x.c;
+    sb[threadIdx.x] = y.s;
+    cb[threadIdx.x] = y.c;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        Comp u, w;
+        for (int k = 0; k < 256; ++k) {
+            u.add(sa[k]);
+            u.add(ca[k]);
+            w.add(sb[k]);
+            w.add(cb[k]);
+        }
+        out[2 * q] = u.value();
+        out[2 * q + 1] = w.value();
+    }
+}
+
+}  // namespace
+}  // namespace sdt
+
+using namespace sdt;
+
+struct sdt_job {
+    Tiling t;
+    std::vector<int64_t> range, spin, sym, offset, alpha;
+    std::vector<double> evl;
+    int dev = 0;
+    // device
+    int32_t *tiles = nullptr;
+    double *evl_d = nullptr;
+    int64_t *pair_off = nullptr;
+    double *arr[DST_N] = {nullptr};
+    size_t arr_n[DST_N] = {0};
+    bool loaded = false;
+    // run workspace
+    int64_t *klist_d = nullptr, *pref_d = nullptr;
+    double *factor_d = nullptr, *part_d = nullptr, *task_d = nullptr, *out_d = nullptr;
+    size_t cap_tasks = 0, cap_items = 0;
+    double *host_out = nullptr;
+    size_t cap_host = 0;
+};
+
+namespace {
+
+void job_free_arrays(sdt_job *j) {
+    for (int a = 0; a < DST_N; ++a) {
+        gpu_put(j->arr[a]);
+        j->arr[a] = nullptr;
+        j->arr_n[a] = 0;
+    }
+}
+
+int tiles_upload(sdt_job *j, cudaStream_t st) {
+    const int64_t nt = j->t.noab + j->t.nvab;
+    std::vector<int32_t> tab(4 * nt);
+    for (int64_t b = 1; b <= nt; ++b) {
+        tab[4 * (b - 1) + 0] = (int32_t)j->t.start(b);
+        tab[4 * (b - 1) + 1] = (int32_t)j->t.r(b);
+        tab[4 * (b - 1) + 2] = (int32_t)j->t.s(b);
+        tab[4 * (b - 1) + 3] = (int32_t)j->t.y(b);
+    }
+    j->tiles = (int32_t *)gpu_get(tab.size() * sizeof(int32_t));
+    j->evl_d = (double *)gpu_get(j->evl.size() * sizeof(double));
+    j->pair_off = (int64_t *)gpu_get((size_t)(j->t.nvab * j->t.nvab) * sizeof(int64_t));
+    if (!j->tiles || !j->evl_d || !j->pair_off) return fail(SDT_ERR_NOMEM, "sdt_job_create: device tables");
+    int rc = cuda_check(cudaMemcpyAsync(j->tiles, tab.data(), tab.size() * sizeof(int32_t),
+                                        cudaMemcpyHostToDevice, st), "sdt_job_create");
+    if (rc) return rc;
+    rc = cuda_check(cudaMemcpyAsync(j->evl_d, j->evl.data(), j->evl.size() * sizeof(double),
+                                    cudaMemcpyHostToDevice, st), "sdt_job_create");
+    if (rc) return rc;
+    return cuda_check(cudaStreamSynchronize(st), "sdt_job_create");
+}
+
+// restricted beta->alpha mapping of a tile quad (tce_restricted.F:28-71).
+void restrict4(const Tiling &t, int64_t *b, int n) {
+    int64_t s = 0;
+    for (int q = 0; q < n; ++q) s += t.s(b[q]);
+    if (t.restricted && s == 2 * n)
+        for (int q = 0; q < n; ++q) b[q] = t.alpha[b[q] - 1];
+}
+
+}  // namespace
+
+extern "C" int sdt_job_create(const sdt_tiling *ti, sdt_job **out) {
+    if (!out) return fail(SDT_ERR_ARG, "sdt_job_create: null output");
+    *out = nullptr;
+    Tiling tt;
+    if (!make_tiling(ti, &tt)) return fail(SDT_ERR_ARG, "sdt_job_create: bad tiling");
+    if (tt.noab + tt.nvab > kMaxTiles) return fail(SDT_ERR_ARG, "sdt_job_create: more than 256 tiles");
+    sdt_job *j = new sdt_job();
+    const int64_t nt = tt.noab + tt.nvab;
+    j->range.assign(ti->range, ti->range + nt);
+    j->spin.assign(ti->spin, ti->spin + nt);
+    j->sym.assign(ti->sym, ti->sym + nt);
+    j->offset.assign(ti->offset, ti->offset + nt);
+    if (ti->alpha) j->alpha.assign(ti->alpha, ti->alpha + nt);
+    j->t = tt;
+    j->evl.assign(ti->evl_sorted, ti->evl_sorted + (tt.nocc + tt.nvir));
+    j->t.range = j->range.data();
+    j->t.spin = j->spin.data();
+    j->t.sym = j->sym.data();
+    j->t.offset = j->offset.data();
+    j->t.alpha = j->alpha.empty() ? nullptr : j->alpha.data();
+    j->t.evl = j->evl.data();
+    cudaGetDevice(&j->dev);
+    cudaStream_t st = lib_stream();
+    if (!st) {
+        delete j;
+        return fail(SDT_ERR_CUDA, "sdt_job_create: no stream");
+    }
+    int rc = tiles_upload(j, st);
+    if (rc) {
+        sdt_job_destroy(j);
+        return rc;
+    }
+    *out = j;
+    return SDT_OK;
+}
+
+extern "C" int64_t sdt_job_device_bytes(const sdt_job *j) {
+    if (!j) return 0;
+    int64_t b = 0;
+    for (int a = 0; a < DST_N; ++a) b += (int64_t)j->arr_n[a] * 8;
+    return b;
+}
+
+extern "C" int sdt_job_load(sdt_job *j, const sdt_file *f1, const sdt_file *f2,
+                            const sdt_file *fv, void *stream) {
+    if (!j || !f1 || !f2 || !fv || !f1->hash || !f2->hash || !fv->hash)
+        return fail(SDT_ERR_ARG, "sdt_job_load: null argument");
+    cudaStream_t st = stream ? (cudaStream_t)stream : lib_stream();
+    const Tiling &t = j->t;
+    const int64_t o = t.nocc, v = t.nvir, noab = t.noab, nvab = t.nvab, N = noab + nvab;
+
+    // Virtual tile-pair regions of Vd2.
+    std::vector<int64_t> pair(nvab * nvab, -1);
+    int64_t vd2 = 0;
+    for (int64_t B = noab + 1; B <= N; ++B)
+        for (int64_t C = B; C <= N; ++C) {
+            pair[(B - noab - 1) * nvab + (C - noab - 1)] = vd2;
+            vd2 += t.r(B) * t.r(C) * o * v;
+        }
+    const size_t want[DST_N] = {(size_t)(v * o), (size_t)(v * v * o * o), (size_t)(v * v * o * o),
+                                (size_t)vd2, (size_t)(v * o * o * o), (size_t)(v * v * o * o)};
+    job_free_arrays(j);
+    j->loaded = false;
+    for (int a = 0; a < DST_N; ++a) {
+        j->arr[a] = (double *)gpu_get(want[a] * sizeof(double));
+        if (!j->arr[a]) {
+            job_free_arrays(j);
+            return fail(SDT_ERR_NOMEM, "sdt_job_load: dense operand allocation");
+        }
+        j->arr_n[a] = want[a];
+        int rc = cuda_check(cudaMemsetAsync(j->arr[a], 0, want[a] * sizeof(double), st), "sdt_job_load");
+        if (rc) return rc;
+    }
+    int rc = cuda_check(cudaMemcpyAsync(j->pair_off, pair.data(), pair.size() * sizeof(int64_t),
+                                        cudaMemcpyHostToDevice, st), "sdt_job_load");
+    if (rc) return rc;
+
+    // Copy jobs, destination-driven: every canonical block the path can
+    // read is looked up by its (restricted-mapped) key.
+    std::vector<CopyJob> jobs;
+    std::string missing;
+    auto lookup = [&](const sdt_file *f, int64_t key) {
+        const int64_t off = hash_lookup(f->hash, key);
+        if (off < 0 && missing.empty()) missing = "key " + std::to_string(key);
+        return off;
+    };
+    auto add = [&](int file, int dst, int64_t src_block, int64_t n0, int64_t n1, int64_t n2,
+                   int64_t n3, int64_t d0, int64_t s0, int64_t s1, int64_t s2, int64_t s3, double sign) {
+        // one job per leading index x0 (keeps each CTA's slab moderate)
+        for (int64_t x0 = 0; x0 < n0; ++x0) {
+            CopyJob c;
+            c.src = src_block + x0 * n1 * n2 * n3;
+            c.dst = d0 + x0 * s0;
+            c.n1 = n1; c.n2 = n2; c.n3 = n3;
+            c.s1 = s1; c.s2 = s2; c.s3 = s3;
+            c.sign = sign;
+            c.src_file = file;
+            c.dst_array = dst;
+            jobs.push_back(c);
+        }
+    };
+    auto spin_ok = [&](int64_t a, int64_t b, int64_t c, int64_t d) {
+        return t.s(a) + t.s(b) == t.s(c) + t.s(d) && (t.y(a) ^ t.y(b) ^ t.y(c) ^ t.y(d)) == 0;
+    };
+    // T1 (p,h): ccsd_t_singles_l.F:341-350 (sorted to t1sub(p4,h1)).
+    for (int64_t p = noab + 1; p <= N; ++p)
+        for (int64_t h = 1; h <= noab; ++h) {
+            if (t.s(p) != t.s(h) || (t.y(p) ^ t.y(h)) != 0) continue;
+            int64_t b[2] = {p, h};
+            restrict4(t, b, 2);
+            const int64_t off = lookup(f1, b[1] - 1 + noab * (b[0] - noab - 1));
+            if (off < 0) continue;
+            add(0, DST_T1, off, 1, 1, t.r(p), t.r(h), t.start(p) * o + t.start(h), 0, 0, o, 1, 1.0);
+        }
+    // T2 (p1<=p2, h3<=h4): direct blocks plus the mirrors tce_hashnsort.F
+    // reads with factor -1 (h7b<h1b for d1, p7b<p4b for d2).
+    for (int64_t p1 = noab + 1; p1 <= N; ++p1)
+        for (int64_t p2 = p1; p2 <= N; ++p2)
+            for (int64_t h3 = 1; h3 <= noab; ++h3)
+                for (int64_t h4 = h3; h4 <= noab; ++h4) {
+                    if (!spin_ok(p1, p2, h3, h4)) continue;
+                    int64_t b[4] = {p1, p2, h3, h4};
+                    restrict4(t, b, 4);
+                    const int64_t key = b[3] - 1 + noab * (b[2] - 1 + noab * (b[1] - noab - 1 + nvab * (b[0] - noab - 1)));
+                    const int64_t off = lookup(f2, key);
+                    if (off < 0) continue;
+                    const int64_t n0 = t.r(p1), n1 = t.r(p2), n2 = t.r(h3), n3 = t.r(h4);
+                    const int64_t P1 = t.start(p1), P2 = t.start(p2), H3 = t.start(h3), H4 = t.start(h4);
+                    // T2a[p][q][h][l]: strides v*o*o, o*o, o, 1
+                    const int64_t ap = v * o * o, aq = o * o, ah = o, al = 1;
+                    add(1, DST_T2A, off, n0, n1, n2, n3, P1 * ap + P2 * aq + H3 * ah + H4 * al, ap, aq, ah, al, 1.0);
+                    if (h3 != h4)
+                        add(1, DST_T2A, off, n0, n1, n2, n3, P1 * ap + P2 * aq + H4 * ah + H3 * al, ap, aq, al, ah, -1.0);
+                    // T2b[p][h][l][q]: strides o*o*v, o*v, v, 1
+                    const int64_t bp = o * o * v, bh = o * v, bl = v, bq = 1;
+                    add(1, DST_T2B, off, n0, n1, n2, n3, P1 * bp + H3 * bh + H4 * bl + P2 * bq, bp, bq, bh, bl, 1.0);
+                    if (p1 != p2)
+                        add(1, DST_T2B, off, n0, n1, n2, n3, P2 * bp + H3 * bh + H4 * bl + P1 * bq, bq, bp, bh, bl, -1.0);
+                }
+    // V2 <p5 p6||h3 p7> (p5<=p6): Vd2 region of the pair, [b][c][k][e].
+    for (int64_t p5 = noab + 1; p5 <= N; ++p5)
+        for (int64_t p6 = p5; p6 <= N; ++p6)
+            for (int64_t h3 = 1; h3 <= noab; ++h3)
+                for (int64_t p7 = noab + 1; p7 <= N; ++p7) {
+                    if (!spin_ok(p5, p6, h3, p7)) continue;
+                    int64_t b[4] = {p5, p6, h3, p7};
+                    restrict4(t, b, 4);
+                    const int64_t off = lookup(fv, b[3] - 1 + N * (b[2] - 1 + N * (b[1] - 1 + N * (b[0] - 1))));
+                    if (off < 0) continue;
+                    const int64_t n1 = t.r(p6);
+                    const int64_t base = pair[(p5 - noab - 1) * nvab + (p6 - noab - 1)] + t.start(h3) * v + t.start(p7);
+                    add(2, DST_VD2, off, t.r(p5), n1, t.r(h3), t.r(p7), base, n1 * o * v, o * v, v, 1, 1.0);
+                }
+    // V2 <h7 p6||h2 h3> (h2<=h3): Wd1[c][j][k][m].
+    for (int64_t h7 = 1; h7 <= noab; ++h7)
+        for (int64_t p6 = noab + 1; p6 <= N; ++p6)
+            for (int64_t h2 = 1; h2 <= noab; ++h2)
+                for (int64_t h3 = h2; h3 <= noab; ++h3) {
+                    if (!spin_ok(h7, p6, h2, h3)) continue;
+                    int64_t b[4] = {h7, p6, h2, h3};
+                    restrict4(t, b, 4);
+                    const int64_t off = lookup(fv, b[3] - 1 + N * (b[2] - 1 + N * (b[1] - 1 + N * (b[0] - 1))));
+                    if (off < 0) continue;
+                    const int64_t base = ((t.start(p6) * o + t.start(h2)) * o + t.start(h3)) * o + t.start(h7);
+                    // key order (m, c, j, k): strides 1, o^3, o^2, o
+                    add(2, DST_WD1, off, t.r(h7), t.r(p6), t.r(h2), t.r(h3), base, 1, o * o * o, o * o, o, 1.0);
+                }
+    // V2 <p5 p6||h2 h3> (p5<=p6, h2<=h3): Ud[b][c][j][k].
+    for (int64_t p5 = noab + 1; p5 <= N; ++p5)
+        for (int64_t p6 = p5; p6 <= N; ++p6)
+            for (int64_t h2 = 1; h2 <= noab; ++h2)
+                for (int64_t h3 = h2; h3 <= noab; ++h3) {
+                    if (!spin_ok(p5, p6, h2, h3)) continue;
+                    int64_t b[4] = {p5, p6, h2, h3};
+                    restrict4(t, b, 4);
+                    const int64_t off = lookup(fv, b[3] - 1 + N * (b[2] - 1 + N * (b[1] - 1 + N * (b[0] - 1))));
+                    if (off < 0) continue;
+                    const int64_t base = ((t.start(p5) * v + t.start(p6)) * o + t.start(h2)) * o + t.start(h3);
+                    add(2, DST_UD, off, t.r(p5), t.r(p6), t.r(h2), t.r(h3), base, v * o * o, o * o, o, 1, 1.0);
+                }
+    if (!missing.empty()) {
+        job_free_arrays(j);
+        return fail(SDT_ERR_MISSING, "sdt_job_load: a block the path reads is absent (" + missing + ")");
+    }
+
+    // Raw files to the device, then one ingest launch per 65535 jobs.
+    const sdt_file *files[3] = {f1, f2, fv};
+    double *raw[3] = {nullptr, nullptr, nullptr};
+    for (int f = 0; f < 3; ++f) {
+        raw[f] = (double *)gpu_get((size_t)std::max<int64_t>(files[f]->ndata, 1) * sizeof(double));
+        if (!raw[f]) {
+            for (int g = 0; g < f; ++g) gpu_put(raw[g]);
+            job_free_arrays(j);
+            return fail(SDT_ERR_NOMEM, "sdt_job_load: raw file allocation");
+        }
+        if (files[f]->ndata > 0) {
+            rc = cuda_check(cudaMemcpyAsync(raw[f], files[f]->data, (size_t)files[f]->ndata * sizeof(double),
+                                            cudaMemcpyHostToDevice, st), "sdt_job_load");
+            if (rc) return rc;
+        }
+    }
+    CopyJob *jobs_d = (CopyJob *)gpu_get(std::max<size_t>(jobs.size(), 1) * sizeof(CopyJob));
+    if (!jobs_d) return fail(SDT_ERR_NOMEM, "sdt_job_load: job list");
+    rc = cuda_check(cudaMemcpyAsync(jobs_d, jobs.data(), jobs.size() * sizeof(CopyJob),
+                                    cudaMemcpyHostToDevice, st), "sdt_job_load");
+    if (rc) return rc;
+    IngestArgs g;
+    for (int f = 0; f < 3; ++f) g.src[f] = raw[f];
+    for (int a = 0; a < DST_N; ++a) g.dst[a] = j->arr[a];
+    for (size_t b0 = 0; b0 < jobs.size(); b0 += 65535) {
+        g.jobs = jobs_d + b0;
+        const unsigned nb = (unsigned)std::min<size_t>(65535, jobs.size() - b0);
+        ingest_kernel<<<nb, 256, 0, st>>>(g);
+        count_launch();
+    }
+    rc = cuda_check(cudaGetLastError(), "sdt_job_load: ingest");
+    // The raw copies and the job list are released once the stream is done.
+    cudaError_t e = cudaStreamSynchronize(st);
+    for (int f = 0; f < 3; ++f) gpu_put(raw[f]);
+    gpu_put(jobs_d);
+    if (rc) return rc;
+    rc = cuda_check(e, "sdt_job_load: ingest");
+    if (rc) return rc;
+    j->loaded = true;
+    return SDT_OK;
+}
+
+namespace {
+// Multiplicity factor of a tuple (ccsd_t_dot.F:52-66).
+double tuple_factor(const int64_t *k, bool restricted) {
+    double f = restricted ? 2.0 : 1.0;
+    if (k[0] == k[1] && k[1] == k[2]) f /= 6.0;
+    else if (k[0] == k[1] || k[1] == k[2]) f /= 2.0;
+    if (k[3] == k[4] && k[4] == k[5]) f /= 6.0;
+    else if (k[3] == k[4] || k[4] == k[5]) f /= 2.0;
+    return f;
+}
+
+bool grow(void **p, size_t *cap, size_t bytes) {
+    if (*cap >= bytes && *p) return true;
+    gpu_put(*p);
+    *p = gpu_get(bytes);
+    *cap = *p ? bytes : 0;
+    return *p != nullptr;
+}
+}  // namespace
+
+extern "C" int sdt_job_run(sdt_job *j, const int64_t *klist, int64_t n, int precision,
+                           double *energy, double *per_task, void *stream) {
+    if (!j || !energy || (n > 0 && !klist)) return fail(SDT_ERR_ARG, "sdt_job_run: null argument");
+    if (!j->loaded) return fail(SDT_ERR_STATE, "sdt_job_run: sdt_job_load has not succeeded");
+    if (precision != SDT_PREC_FP64) return fail(SDT_ERR_ARG, "sdt_job_run: unknown precision");
+    energy[0] = energy[1] = 0.0;
+    if (n == 0) return SDT_OK;
+    cudaStream_t st = stream ? (cudaStream_t)stream : lib_stream();
+    const Tiling &t = j->t;
+    const int64_t nt = t.noab + t.nvab;
+    std::vector<int64_t> pref(n + 1, 0);
+    std::vector<double> fac(n);
+    for (int64_t q = 0; q < n; ++q) {
+        const int64_t *k = klist + 7 * q;
+        int64_t boxes = 1;
+        for (int d = 0; d < 6; ++d) {
+            const bool virt = d < 3;
+            if (k[d] < 1 || k[d] > nt || (virt ? k[d] <= t.noab : k[d] > t.noab))
+                return fail(SDT_ERR_ARG, "sdt_job_run: tuple tile out of range");
+            boxes *= (t.r(k[d]) + BOX - 1) / BOX;
+        }
+        if (!(k[0] <= k[1] && k[1] <= k[2] && k[3] <= k[4] && k[4] <= k[5]))
+            return fail(SDT_ERR_ARG, "sdt_job_run: tuple tiles not sorted");
+        pref[q + 1] = pref[q] + boxes;
+        fac[q] = tuple_factor(k, t.restricted != 0);
+    }
+    const int64_t items = pref[n];
+    void *p0 = j->klist_d, *p1 = j->pref_d, *p2 = j->factor_d, *p3 = j->task_d, *p4 = j->part_d;
+    size_t c_tasks = j->cap_tasks, c_items = j->cap_items;
+    // Workspace sized by the largest request so far.
+    if (c_tasks < (size_t)n || !p0) {
+        size_t cap = 0;
+        bool ok = grow(&p0, &cap, 7 * n * sizeof(int64_t));
+        cap = 0; ok = ok && grow(&p1, &cap, (n + 1) * sizeof(int64_t));
+        cap = 0; ok = ok && grow(&p2, &cap, n * sizeof(double));
+        cap = 0; ok = ok && grow(&p3, &cap, 2 * n * sizeof(double));
+        if (!ok) return fail(SDT_ERR_NOMEM, "sdt_job_run: workspace");
+        c_tasks = n;
+    }
+    if (c_items < (size_t)items || !p4) {
+        size_t cap = 0;
+        if (!grow(&p4, &cap, 2 * items * sizeof(double))) return fail(SDT_ERR_NOMEM, "sdt_job_run: partials");
+        c_items = items;
+    }
+    j->klist_d = (int64_t *)p0; j->pref_d = (int64_t *)p1; j->factor_d = (double *)p2;
+    j->task_d = (double *)p3; j->part_d = (double *)p4;
+    j->cap_tasks = c_tasks; j->cap_items = c_items;
+    if (!j->out_d) j->out_d = (double *)gpu_get(2 * sizeof(double));
+    const size_t hbytes = (2 * n + 2) * sizeof(double);
+    if (j->cap_host < hbytes) {
+        host_put(j->host_out);
+        j->host_out = (double *)host_get(hbytes);
+        j->cap_host = j->host_out ? hbytes : 0;
+    }
+    if (!j->out_d || !j->host_out) return fail(SDT_ERR_NOMEM, "sdt_job_run: output buffers");
+
+    int rc = cuda_check(cudaMemcpyAsync(j->klist_d, klist, 7 * n * sizeof(int64_t), cudaMemcpyHostToDevice, st), "sdt_job_run");
+    if (!rc) rc = cuda_check(cudaMemcpyAsync(j->pref_d, pref.data(), (n + 1) * sizeof(int64_t), cudaMemcpyHostToDevice, st), "sdt_job_run");
+    if (!rc) rc = cuda_check(cudaMemcpyAsync(j->factor_d, fac.data(), n * sizeof(double), cudaMemcpyHostToDevice, st), "sdt_job_run");
+    if (rc) return rc;
+
+    FusedParams p;
+    p.T1d = j->arr[DST_T1]; p.T2a = j->arr[DST_T2A]; p.T2b = j->arr[DST_T2B];
+    p.Vd2 = j->arr[DST_VD2]; p.Wd1 = j->arr[DST_WD1]; p.Ud = j->arr[DST_UD];
+    p.pair_off = j->pair_off;
+    p.evl = j->evl_d;
+    p.tiles = j->tiles;
+    p.noab = (int32_t)t.noab; p.nvab = (int32_t)t.nvab;
+    p.nocc = t.nocc; p.nvir = t.nvir;
+    p.klist = j->klist_d; p.item_pref = j->pref_d; p.factor = j->factor_d;
+    p.n_tasks = n;
+    p.part = j->part_d;
+    const int64_t chunk = 1ll << 30;
+    for (int64_t b0 = 0; b0 < items; b0 += chunk) {
+        p.item_base = b0;
+        const unsigned nb = (unsigned)std::min<int64_t>(chunk, items - b0);
+        fused_fp64_kernel<<<nb, kThreads, 0, st>>>(p);
+        count_launch();
+    }
+    rc = cuda_check(cudaGetLastError(), "sdt_job_run: fused kernel");
+    if (rc) return rc;
+    for (int64_t q0 = 0; q0 < n; q0 += 65535) {
+        const unsigned nb = (unsigned)std::min<int64_t>(65535, n - q0);
+        tuple_sum_kernel<<<nb, 256, 0, st>>>(j->part_d, j->pref_d + q0, nb, j->task_d + 2 * q0);
+        count_launch();
+    }
+    rc = reduce_pairs(j->task_d, n, j->out_d, st);
+    if (rc) return rc;
+    rc = cuda_check(cudaMemcpyAsync(j->host_out, j->out_d, 2 * sizeof(double), cudaMemcpyDeviceToHost, st), "sdt_job_run");
+    if (!rc && per_task)
+        rc = cuda_check(cudaMemcpyAsync(j->host_out + 2, j->task_d, 2 * n * sizeof(double), cudaMemcpyDeviceToHost, st), "sdt_job_run");
+    if (rc) return rc;
+    rc = cuda_check(cudaStreamSynchronize(st), "sdt_job_run");
+    if (rc) return rc;
+    energy[0] = j->host_out[0];
+    energy[1] = j->host_out[1];
+    if (per_task) std::memcpy(per_task, j->host_out + 2, 2 * n * sizeof(double));
+    return SDT_OK;
+}
+
+extern "C" int sdt_job_destroy(sdt_job *j) {
+    if (!j) return SDT_OK;
+    cudaStreamSynchronize(lib_stream());
+    job_free_arrays(j);
+    gpu_put(j->tiles);
+    gpu_put(j->evl_d);
+    gpu_put(j->pair_off);
+    gpu_put(j->klist_d);
+    gpu_put(j->pref_d);
+    gpu_put(j->factor_d);
+    gpu_put(j->part_d);
+    gpu_put(j->task_d);
+    gpu_put(j->out_d);
+    host_put(j->host_out);
+    delete j;
+    return SDT_OK;
+}
+
+extern "C" int sdt_ccsd_t(const sdt_tiling *t, const sdt_file *t1, const sdt_file *t2,
+                          const sdt_file *v2, double *energy1, double *energy2) {
+    if (!energy1 || !energy2) return fail(SDT_ERR_ARG, "sdt_ccsd_t: null output");
+    const int64_t n = sdt_tasks_count(t);
+    if (n < 0) return SDT_ERR_ARG;
+    std::vector<int64_t> klist(7 * std::max<int64_t>(n, 1));
+    int rc = sdt_tasks_list(t, n, klist.data());
+    if (rc) return rc;
+    sdt_job *j = nullptr;
+    rc = sdt_job_create(t, &j);
+    if (rc) return rc;
+    rc = sdt_job_load(j, t1, t2, v2, nullptr);
+    double e[2] = {0.0, 0.0};
+    if (!rc) rc = sdt_job_run(j, klist.data(), n, SDT_PREC_FP64, e, nullptr, nullptr);
+    sdt_job_destroy(j);
+    if (rc) return rc;
+    *energy1 = e[0];
+    *energy2 = e[1];
+    return SDT_OK;
+}

@@ -1,0 +1,195 @@
+// sdt_mem.cu -- caching allocator, library stream, device binding and the
+// deterministic pair reduction shared by both surfaces.
+//
+// Replaces src/tce/ccsd_t/memory.cu (initmemmodule_, getGpuMem, getHostMem,
+// freeGpuMem, freeHostMem, finalizememmodule_) and src/tce/ccsd_t/hybrid.c
+// (check_device_, device_init_).
+#include "sdt_common.cuh"
+
+#include <cstdio>
+#include <cstdlib>
+#include <map>
+#include <mutex>
+
+namespace sdt {
+
+namespace {
+struct Pool {
+    std::multimap<size_t, void *> free_dev, free_host;
+    std::map<void *, size_t> live_dev, live_host;
+    bool init = false;
+};
+Pool &pool() {
+    static Pool p;
+    return p;
+}
+std::mutex &pool_mu() {
+    static std::mutex m;
+    return m;
+}
+cudaStream_t g_stream = nullptr;
+int g_stream_dev = -1;
+}  // namespace
+
+int cuda_check(cudaError_t e, const char *what) {
+    if (e == cudaSuccess) return SDT_OK;
+    return fail(SDT_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+cudaStream_t lib_stream() {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (!g_stream || g_stream_dev != dev) {
+        cudaStream_t s = nullptr;
+        if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess) return nullptr;
+        g_stream = s;
+        g_stream_dev = dev;
+    }
+    return g_stream;
+}
+
+// Reuse the smallest cached block of at least `bytes`; otherwise allocate.
+static void *take(std::multimap<size_t, void *> &fl, std::map<void *, size_t> &live,
+                  size_t bytes, bool dev) {
+    auto it = fl.lower_bound(bytes);
+    if (it != fl.end() && it->first <= bytes * 2 + (1u << 20)) {
+        void *p = it->second;
+        live[p] = it->first;
+        fl.erase(it);
+        return p;
+    }
+    void *p = nullptr;
+    cudaError_t e = dev ? cudaMalloc(&p, bytes) : cudaMallocHost(&p, bytes);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        // Drop the cache and retry once.
+        for (auto &kv : fl) dev ? cudaFree(kv.second) : cudaFreeHost(kv.second);
+        fl.clear();
+        e = dev ? cudaMalloc(&p, bytes) : cudaMallocHost(&p, bytes);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            return nullptr;
+        }
+    }
+    live[p] = bytes;
+    return p;
+}
+
+void *gpu_get(size_t bytes) {
+    std::lock_guard<std::mutex> lk(pool_mu());
+    if (bytes == 0) bytes = 8;
+    return take(pool().free_dev, pool().live_dev, bytes, true);
+}
+void gpu_put(void *p) {
+    if (!p) return;
+    std::lock_guard<std::mutex> lk(pool_mu());
+    auto it = pool().live_dev.find(p);
+    if (it == pool().live_dev.end()) return;
+    pool().free_dev.emplace(it->second, p);
+    pool().live_dev.erase(it);
+}
+void *host_get(size_t bytes) {
+    std::lock_guard<std::mutex> lk(pool_mu());
+    if (bytes == 0) bytes = 8;
+    return take(pool().free_host, pool().live_host, bytes, false);
+}
+void host_put(void *p) {
+    if (!p) return;
+    std::lock_guard<std::mutex> lk(pool_mu());
+    auto it = pool().live_host.find(p);
+    if (it == pool().live_host.end()) return;
+    pool().free_host.emplace(it->second, p);
+    pool().live_host.erase(it);
+}
+
+// ---------------------------------------------------------------------------
+// Deterministic sum of n (E[T], E(T)) pairs: one block, fixed thread count,
+// each thread a Neumaier sum over a fixed stride, then a fixed-order tree.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) reduce_pairs_kernel(const double *__restrict__ part,
+                                                           int64_t n, double *__restrict__ out) {
+    __shared__ double s1[256], c1[256], s2[256], c2[256];
+    Comp a, b;
+    for (int64_t i = threadIdx.x; i < n; i += 256) {
+        a.add(part[2 * i]);
+        b.add(part[2 * i + 1]);
+    }
+    s1[threadIdx.x] = a.s;
+    c1[threadIdx.x] = a.c;
+    s2[threadIdx.x] = b.s;
+    c2[threadIdx.x] = b.c;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        Comp x, y;
+        for (int q = 0; q < 256; ++q) {
+            x.add(s1[q]);
+            x.add(c1[q]);
+            y.add(s2[q]);
+            y.add(c2[q]);
+        }
+        out[0] = x.value();
+        out[1] = y.value();
+    }
+}
+
+int reduce_pairs(const double *partials, int64_t n, double *out_dev, cudaStream_t st) {
+    reduce_pairs_kernel<<<1, 256, 0, st>>>(partials, n, out_dev);
+    count_launch();
+    return cuda_check(cudaGetLastError(), "reduce_pairs");
+}
+
+static int local_index() {
+    const char *names[] = {"SDT_LOCAL_RANK", "LOCAL_RANK", "OMPI_COMM_WORLD_LOCAL_RANK",
+                           "MPI_LOCALRANKID", "SLURM_LOCALID"};
+    for (const char *n : names) {
+        const char *v = std::getenv(n);
+        if (v && *v) return std::atoi(v);
+    }
+    return 0;
+}
+
+}  // namespace sdt
+
+using namespace sdt;
+
+extern "C" void initmemmodule_(void) {
+    std::lock_guard<std::mutex> lk(pool_mu());
+    pool().init = true;
+}
+
+extern "C" void finalizememmodule_(void) {
+    bool leaked;
+    {
+        std::lock_guard<std::mutex> lk(pool_mu());
+        leaked = !pool().live_host.empty() || !pool().live_dev.empty();
+        pool().init = false;
+        // Freed blocks stay cached for the next tuple; memory.cu returns them
+        // to the driver here, which costs a cudaFree/cudaMalloc per tuple.
+    }
+    if (leaked) {
+        fail(SDT_ERR_STATE, "finalizememmodule_: live device or host blocks remain");
+        fortran_abort_if_exit_mode();
+    }
+}
+
+extern "C" int check_device_(long *icuda) {
+    if (!icuda) return 0;
+    return local_index() < *icuda ? 1 : 0;
+}
+
+extern "C" int device_init_(long *icuda, long *cuda_device_number) {
+    int count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess) {
+        cudaGetLastError();
+        count = 0;
+    }
+    if (!icuda || count < *icuda) {
+        std::printf("Warning: Please check whether you have %ld cuda devices per node\n",
+                    icuda ? *icuda : 0L);
+        std::fflush(stdout);
+        if (cuda_device_number) *cuda_device_number = 30;
+    } else {
+        cudaSetDevice(local_index());
+    }
+    return 1;
+}

@@ -1,0 +1,156 @@
+"""Host-side mirror of NWChem's (T) entry point for the triples tile path.
+
+ccsd_t(tiling, t1, t2, v2) plays the role of the reference's
+ccsd_t(d_t1,k_t1_offset,d_t2,k_t2_offset,d_v2,k_v2_offset,energy1,energy2,
+size_t1) (src/tce/ccsd_t/ccsd_t.F:19-20): the three TCE files go in, E[T]
+(energy1, the "CCSD[T] correction") and E(T) (energy2, the "CCSD(T)
+correction") come out.  E[ST] = E(T) - E[T].
+
+TceFile holds one TCE file in host memory: the tce_hash table (hash[0] = n,
+keys ascending in hash[1..n], block offsets in hash[n+1..2n]) and the block
+data, each block row-major in its key order.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _capi
+from .tiling import Tiling
+
+FILE_T1, FILE_T2, FILE_V2 = 0, 1, 2
+PREC_FP64 = 0
+
+
+@dataclass
+class TceFile:
+    hash: np.ndarray
+    data: np.ndarray
+
+    def struct(self) -> _capi.SdtFile:
+        return _capi.SdtFile(self.hash.ctypes.data_as(_capi.PI64), self.data.ctypes.data_as(_capi.PD),
+                             int(self.data.size))
+
+    @property
+    def nbytes(self) -> int:
+        return int(self.data.nbytes + self.hash.nbytes)
+
+    def lookup(self, key: int) -> int:
+        """Block offset of key (tce_hash), or -1."""
+        n = int(self.hash[0])
+        keys = self.hash[1:n + 1]
+        i = int(np.searchsorted(keys, key))
+        if i < n and keys[i] == key:
+            return int(self.hash[n + 1 + i])
+        return -1
+
+
+def synth_file(tiling: Tiling, kind: int, seed: int, pinned: bool = False) -> TceFile:
+    """Seeded synthetic TCE file (T1, T2 or V2 with its vvov, ovoo and vvoo blocks)."""
+    lib = _capi.lib()
+    ts = tiling.struct()
+    nb, nd = C.c_int64(), C.c_int64()
+    _capi.check(lib.sdt_synth_file(C.byref(ts), kind, seed, C.byref(nb), C.byref(nd), None, None),
+                "sdt_synth_file")
+    h = np.empty(2 * nb.value + 1, dtype=np.int64)
+    if pinned:
+        import torch
+        d = torch.empty(max(nd.value, 1), dtype=torch.float64, pin_memory=True).numpy()[:nd.value]
+    else:
+        d = np.empty(nd.value, dtype=np.float64)
+    _capi.check(lib.sdt_synth_file(C.byref(ts), kind, seed, C.byref(nb), C.byref(nd),
+                                   h.ctypes.data_as(_capi.PI64), d.ctypes.data_as(_capi.PD)),
+                "sdt_synth_file")
+    return TceFile(h, d)
+
+
+def synth_inputs(tiling: Tiling, seed: int, pinned: bool = False) -> tuple[TceFile, TceFile, TceFile]:
+    return tuple(synth_file(tiling, k, seed, pinned) for k in (FILE_T1, FILE_T2, FILE_V2))
+
+
+def task_list(tiling: Tiling) -> np.ndarray:
+    """(n, 7) tuple list in the reference's weight order (ccsd_t_neword)."""
+    lib = _capi.lib()
+    ts = tiling.struct()
+    n = lib.sdt_tasks_count(C.byref(ts))
+    if n < 0:
+        _capi.check(-n, "sdt_tasks_count")
+    kl = np.empty((max(n, 1), 7), dtype=np.int64)
+    _capi.check(lib.sdt_tasks_list(C.byref(ts), n, kl.ctypes.data_as(_capi.PI64)), "sdt_tasks_list")
+    return kl[:n]
+
+
+def flops(tiling: Tiling, klist: np.ndarray) -> float:
+    """Algorithmic FLOPs: sum over tuples of Nt*18*(O_allowed+V_allowed+1)."""
+    kl = np.ascontiguousarray(klist, dtype=np.int64)
+    ts = tiling.struct()
+    return float(_capi.lib().sdt_tasks_flops(C.byref(ts), kl.ctypes.data_as(_capi.PI64), len(kl)))
+
+
+def _stream_ptr(stream) -> C.c_void_p:
+    if stream is None:
+        return C.c_void_p(None)
+    if hasattr(stream, "cuda_stream"):
+        return C.c_void_p(stream.cuda_stream)
+    return C.c_void_p(int(stream))
+
+
+class TriplesJob:
+    """One (T) problem resident on the GPU (T1/T2/V2 and orbital energies)."""
+
+    def __init__(self, tiling: Tiling):
+        self.tiling = tiling
+        self._lib = _capi.lib()
+        self._ts = tiling.struct()
+        h = C.c_void_p()
+        _capi.check(self._lib.sdt_job_create(C.byref(self._ts), C.byref(h)), "sdt_job_create")
+        self._h = h
+
+    def load(self, t1: TceFile, t2: TceFile, v2: TceFile, stream=None) -> None:
+        s = [t1.struct(), t2.struct(), v2.struct()]
+        _capi.check(self._lib.sdt_job_load(self._h, C.byref(s[0]), C.byref(s[1]), C.byref(s[2]),
+                                           _stream_ptr(stream)), "sdt_job_load")
+
+    def run(self, klist: np.ndarray, per_task: bool = False, stream=None, precision: int = PREC_FP64):
+        kl = np.ascontiguousarray(klist, dtype=np.int64).reshape(-1, 7)
+        e = np.zeros(2)
+        pt = np.zeros((len(kl), 2)) if per_task else None
+        _capi.check(self._lib.sdt_job_run(self._h, kl.ctypes.data_as(_capi.PI64), len(kl), precision,
+                                          e.ctypes.data_as(_capi.PD),
+                                          pt.ctypes.data_as(_capi.PD) if per_task else None,
+                                          _stream_ptr(stream)), "sdt_job_run")
+        return (float(e[0]), float(e[1]), pt) if per_task else (float(e[0]), float(e[1]))
+
+    @property
+    def device_bytes(self) -> int:
+        return int(self._lib.sdt_job_device_bytes(self._h))
+
+    def close(self) -> None:
+        if self._h:
+            self._lib.sdt_job_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def ccsd_t(tiling: Tiling, t1: TceFile, t2: TceFile, v2: TceFile) -> tuple[float, float]:
+    """(energy1, energy2) = (E[T], E(T)) for the whole tuple list (ccsd_t.F:19-297)."""
+    lib = _capi.lib()
+    ts = tiling.struct()
+    s = [t1.struct(), t2.struct(), v2.struct()]
+    e1, e2 = C.c_double(), C.c_double()
+    _capi.check(lib.sdt_ccsd_t(C.byref(ts), C.byref(s[0]), C.byref(s[1]), C.byref(s[2]),
+                               C.byref(e1), C.byref(e2)), "sdt_ccsd_t")
+    return e1.value, e2.value
