@@ -83,6 +83,10 @@ void dev_mem_d_(sdt_int *h1d, sdt_int *h2d, sdt_int *h3d, sdt_int *p4d,
                 sdt_int *p5d, sdt_int *p6d);
 void dev_mem_s_(sdt_int *h1d, sdt_int *h2d, sdt_int *h3d, sdt_int *p4d,
                 sdt_int *p5d, sdt_int *p6d);
+/* Copies the current device tiles to host buffers of the tuple size (either
+ * may be NULL).  No reference counterpart: the reference only exposes the
+ * tiles through compute_en_; this read-back exists for parity tests. */
+int sdt_tile_download(double *doubles, double *singles);
 /* Release both tiles (sd_t_total.cu:17-28). */
 void dev_release_(void);
 /* Caching device / pinned-host allocator (memory.cu:69,164-178).  Blocks
@@ -179,6 +183,10 @@ int sdt_job_run(sdt_job *job, const int64_t *klist, int64_t n,
 int sdt_job_destroy(sdt_job *job);
 /* Device bytes held by a job. */
 int64_t sdt_job_device_bytes(const sdt_job *job);
+/* When on, sdt_job_run brackets its fused-kernel launches with CUDA events
+ * on the run's stream; sdt_job_last_kernel_ms returns that interval. */
+int sdt_job_set_timing(sdt_job *job, int on);
+double sdt_job_last_kernel_ms(const sdt_job *job);
 
 /* One-shot replacement for ccsd_t(d_t1,k_t1_offset,d_t2,k_t2_offset,
  * d_v2,k_v2_offset,energy1,energy2,size_t1) (ccsd_t.F:19-20): builds the
@@ -189,6 +197,12 @@ int sdt_ccsd_t(const sdt_tiling *t, const sdt_file *t1, const sdt_file *t2,
 
 /* Kernel launches made by this library since load (all entry points). */
 int64_t sdt_launch_count(void);
+
+/* Measured FP64 tensor-core (mma.sync m8n8k4.f64) throughput of the current
+ * device in TFLOP/s: a register-resident loop of independent MMAs over all
+ * SMs for about `ms` milliseconds.  The roofline denominator of the FP64
+ * form. */
+double sdt_probe_fp64_tflops(int ms);
 
 #ifdef __cplusplus
 }

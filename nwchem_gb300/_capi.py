@@ -54,10 +54,14 @@ def _declare(lib):
         "sdt_ccsd_t": (C.c_int, [C.POINTER(SdtTiling), C.POINTER(SdtFile), C.POINTER(SdtFile),
                                  C.POINTER(SdtFile), PD, PD]),
         "sdt_launch_count": (I64, []),
+        "sdt_job_set_timing": (C.c_int, [C.c_void_p, C.c_int]),
+        "sdt_job_last_kernel_ms": (C.c_double, [C.c_void_p]),
+        "sdt_probe_fp64_tflops": (C.c_double, [C.c_int]),
         "compute_en_": (None, [PD, PD, PD, PD, PD, PD, PD, PD, PI64, PI64, PI64, PI64, PI64, PI64, PD, PD]),
         "dev_mem_d_": (None, [PI64] * 6),
         "dev_mem_s_": (None, [PI64] * 6),
         "dev_release_": (None, []),
+        "sdt_tile_download": (C.c_int, [PD, PD]),
         "initmemmodule_": (None, []),
         "finalizememmodule_": (None, []),
         "check_device_": (C.c_int, [C.POINTER(C.c_long)]),

@@ -388,6 +388,10 @@ struct sdt_job {
     size_t cap_tasks = 0, cap_items = 0;
     double *host_out = nullptr;
     size_t cap_host = 0;
+    // optional CUDA-event timing of the fused launches of the last run
+    bool timing = false;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    float last_ms = 0.0f;
 };
 
 namespace {
@@ -513,10 +517,13 @@ extern "C" int sdt_job_load(sdt_job *j, const sdt_file *f1, const sdt_file *f2,
     // read is looked up by its (restricted-mapped) key.
     std::vector<CopyJob> jobs;
     std::string missing;
-    auto lookup = [&](const sdt_file *f, int64_t key) {
+    // Offset of a block; -1 (and an error) when absent or when the block
+    // would reach past the end of the file's data.
+    auto lookup = [&](const sdt_file *f, int64_t key, int64_t size) {
         const int64_t off = hash_lookup(f->hash, key);
-        if (off < 0 && missing.empty()) missing = "key " + std::to_string(key);
-        return off;
+        if ((off < 0 || off + size > f->ndata) && missing.empty())
+            missing = (off < 0 ? "key " : "out-of-range block for key ") + std::to_string(key);
+        return (off < 0 || off + size > f->ndata) ? (int64_t)-1 : off;
     };
     auto add = [&](int file, int dst, int64_t src_block, int64_t n0, int64_t n1, int64_t n2,
                    int64_t n3, int64_t d0, int64_t s0, int64_t s1, int64_t s2, int64_t s3, double sign) {
@@ -542,7 +549,7 @@ extern "C" int sdt_job_load(sdt_job *j, const sdt_file *f1, const sdt_file *f2,
             if (t.s(p) != t.s(h) || (t.y(p) ^ t.y(h)) != 0) continue;
             int64_t b[2] = {p, h};
             restrict4(t, b, 2);
-            const int64_t off = lookup(f1, b[1] - 1 + noab * (b[0] - noab - 1));
+            const int64_t off = lookup(f1, b[1] - 1 + noab * (b[0] - noab - 1), t.r(p) * t.r(h));
             if (off < 0) continue;
             add(0, DST_T1, off, 1, 1, t.r(p), t.r(h), t.start(p) * o + t.start(h), 0, 0, o, 1, 1.0);
         }
@@ -556,7 +563,7 @@ extern "C" int sdt_job_load(sdt_job *j, const sdt_file *f1, const sdt_file *f2,
                     int64_t b[4] = {p1, p2, h3, h4};
                     restrict4(t, b, 4);
                     const int64_t key = b[3] - 1 + noab * (b[2] - 1 + noab * (b[1] - noab - 1 + nvab * (b[0] - noab - 1)));
-                    const int64_t off = lookup(f2, key);
+                    const int64_t off = lookup(f2, key, t.r(p1) * t.r(p2) * t.r(h3) * t.r(h4));
                     if (off < 0) continue;
                     const int64_t n0 = t.r(p1), n1 = t.r(p2), n2 = t.r(h3), n3 = t.r(h4);
                     const int64_t P1 = t.start(p1), P2 = t.start(p2), H3 = t.start(h3), H4 = t.start(h4);
@@ -579,7 +586,8 @@ extern "C" int sdt_job_load(sdt_job *j, const sdt_file *f1, const sdt_file *f2,
                     if (!spin_ok(p5, p6, h3, p7)) continue;
                     int64_t b[4] = {p5, p6, h3, p7};
                     restrict4(t, b, 4);
-                    const int64_t off = lookup(fv, b[3] - 1 + N * (b[2] - 1 + N * (b[1] - 1 + N * (b[0] - 1))));
+                    const int64_t off = lookup(fv, b[3] - 1 + N * (b[2] - 1 + N * (b[1] - 1 + N * (b[0] - 1))),
+                                               t.r(p5) * t.r(p6) * t.r(h3) * t.r(p7));
                     if (off < 0) continue;
                     const int64_t n1 = t.r(p6);
                     const int64_t base = pair[(p5 - noab - 1) * nvab + (p6 - noab - 1)] + t.start(h3) * v + t.start(p7);
@@ -593,7 +601,8 @@ extern "C" int sdt_job_load(sdt_job *j, const sdt_file *f1, const sdt_file *f2,
                     if (!spin_ok(h7, p6, h2, h3)) continue;
                     int64_t b[4] = {h7, p6, h2, h3};
                     restrict4(t, b, 4);
-                    const int64_t off = lookup(fv, b[3] - 1 + N * (b[2] - 1 + N * (b[1] - 1 + N * (b[0] - 1))));
+                    const int64_t off = lookup(fv, b[3] - 1 + N * (b[2] - 1 + N * (b[1] - 1 + N * (b[0] - 1))),
+                                               t.r(h7) * t.r(p6) * t.r(h2) * t.r(h3));
                     if (off < 0) continue;
                     const int64_t base = ((t.start(p6) * o + t.start(h2)) * o + t.start(h3)) * o + t.start(h7);
                     // key order (m, c, j, k): strides 1, o^3, o^2, o
@@ -607,7 +616,8 @@ extern "C" int sdt_job_load(sdt_job *j, const sdt_file *f1, const sdt_file *f2,
                     if (!spin_ok(p5, p6, h2, h3)) continue;
                     int64_t b[4] = {p5, p6, h2, h3};
                     restrict4(t, b, 4);
-                    const int64_t off = lookup(fv, b[3] - 1 + N * (b[2] - 1 + N * (b[1] - 1 + N * (b[0] - 1))));
+                    const int64_t off = lookup(fv, b[3] - 1 + N * (b[2] - 1 + N * (b[1] - 1 + N * (b[0] - 1))),
+                                               t.r(p5) * t.r(p6) * t.r(h2) * t.r(h3));
                     if (off < 0) continue;
                     const int64_t base = ((t.start(p5) * v + t.start(p6)) * o + t.start(h2)) * o + t.start(h3);
                     add(2, DST_UD, off, t.r(p5), t.r(p6), t.r(h2), t.r(h3), base, v * o * o, o * o, o, 1, 1.0);
@@ -752,12 +762,18 @@ extern "C" int sdt_job_run(sdt_job *j, const int64_t *klist, int64_t n, int prec
     p.n_tasks = n;
     p.part = j->part_d;
     const int64_t chunk = 1ll << 30;
+    if (j->timing) {
+        if (!j->ev0) cudaEventCreate(&j->ev0);
+        if (!j->ev1) cudaEventCreate(&j->ev1);
+        cudaEventRecord(j->ev0, st);
+    }
     for (int64_t b0 = 0; b0 < items; b0 += chunk) {
         p.item_base = b0;
         const unsigned nb = (unsigned)std::min<int64_t>(chunk, items - b0);
         fused_fp64_kernel<<<nb, kThreads, 0, st>>>(p);
         count_launch();
     }
+    if (j->timing) cudaEventRecord(j->ev1, st);
     rc = cuda_check(cudaGetLastError(), "sdt_job_run: fused kernel");
     if (rc) return rc;
     for (int64_t q0 = 0; q0 < n; q0 += 65535) {
@@ -773,6 +789,7 @@ extern "C" int sdt_job_run(sdt_job *j, const int64_t *klist, int64_t n, int prec
     if (rc) return rc;
     rc = cuda_check(cudaStreamSynchronize(st), "sdt_job_run");
     if (rc) return rc;
+    if (j->timing) cudaEventElapsedTime(&j->last_ms, j->ev0, j->ev1);
     energy[0] = j->host_out[0];
     energy[1] = j->host_out[1];
     if (per_task) std::memcpy(per_task, j->host_out + 2, 2 * n * sizeof(double));
@@ -793,6 +810,8 @@ extern "C" int sdt_job_destroy(sdt_job *j) {
     gpu_put(j->task_d);
     gpu_put(j->out_d);
     host_put(j->host_out);
+    if (j->ev0) cudaEventDestroy(j->ev0);
+    if (j->ev1) cudaEventDestroy(j->ev1);
     delete j;
     return SDT_OK;
 }
@@ -817,3 +836,11 @@ extern "C" int sdt_ccsd_t(const sdt_tiling *t, const sdt_file *t1, const sdt_fil
     *energy2 = e[1];
     return SDT_OK;
 }
+
+extern "C" int sdt_job_set_timing(sdt_job *j, int on) {
+    if (!j) return fail(SDT_ERR_ARG, "sdt_job_set_timing: null job");
+    j->timing = on != 0;
+    return SDT_OK;
+}
+
+extern "C" double sdt_job_last_kernel_ms(const sdt_job *j) { return j ? (double)j->last_ms : -1.0; }

@@ -463,3 +463,20 @@ extern "C" void compute_en_(double *factor, double *energy, double *eval1, doubl
     energy[0] = out[0];
     energy[1] = out[1];
 }
+
+extern "C" int sdt_tile_download(double *doubles, double *singles) {
+    cudaStream_t st = lib_stream();
+    int rc = SDT_OK;
+    if (doubles) {
+        if (!g_tile.t3) return fail(SDT_ERR_STATE, "sdt_tile_download: no doubles tile");
+        rc = cuda_check(cudaMemcpyAsync(doubles, g_tile.t3, (size_t)g_tile.n3 * sizeof(double),
+                                        cudaMemcpyDeviceToHost, st), "sdt_tile_download");
+    }
+    if (!rc && singles) {
+        if (!g_tile.t3s) return fail(SDT_ERR_STATE, "sdt_tile_download: no singles tile");
+        rc = cuda_check(cudaMemcpyAsync(singles, g_tile.t3s, (size_t)g_tile.n3s * sizeof(double),
+                                        cudaMemcpyDeviceToHost, st), "sdt_tile_download");
+    }
+    if (rc) return rc;
+    return cuda_check(cudaStreamSynchronize(st), "sdt_tile_download");
+}

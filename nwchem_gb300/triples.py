@@ -123,6 +123,14 @@ class TriplesJob:
                                           _stream_ptr(stream)), "sdt_job_run")
         return (float(e[0]), float(e[1]), pt) if per_task else (float(e[0]), float(e[1]))
 
+    def set_timing(self, on: bool = True) -> None:
+        """Bracket the fused launches of each run with CUDA events."""
+        _capi.check(self._lib.sdt_job_set_timing(self._h, 1 if on else 0), "sdt_job_set_timing")
+
+    @property
+    def last_kernel_ms(self) -> float:
+        return float(self._lib.sdt_job_last_kernel_ms(self._h))
+
     @property
     def device_bytes(self) -> int:
         return int(self._lib.sdt_job_device_bytes(self._h))

@@ -19,7 +19,7 @@
  *   orc_singles_l_1       src/tce/ccsd_t/ccsd_t_singles_l.F:30-464
  *   orc_doubles_l_12      src/tce/ccsd_t/offl_ccsd_t_doubles_l.F:72-1020
  *   hashnsort/_2          src/tce/ccsd_t/tce_hashnsort.F:1-173
- *   orc_ccsd_t_dot        src/tce/ccsd_t/ccsd_t_dot.F:20-138
+ *   orc_ccsd_t_dot        src/tce/ccsd_t/ccsd_t_dot.F:20-138 (compensated sums)
  *   orc_6tasks/neword     src/tce/ccsd_t/ccsd_t_neword.F:1-244
  *   orc_ccsd_t            src/tce/ccsd_t/ccsd_t.F:150-297, 358-456
  *
@@ -31,6 +31,7 @@
  * the identity for rank 0 and only changes rounding otherwise.
  */
 #include "sdt_oracle.h"
+#include <math.h>
 #include <stdlib.h>
 #include <string.h>
 
@@ -878,9 +879,19 @@ I orc_tuple_drive(const orc_tiling *t, const orc_file *t1f,
 }
 
 /* ======================================================================
- * ccsd_t_dot (ccsd_t_dot.F:20-138).  Sequential in the reference's loop
- * order so that the sum is deterministic.
+ * ccsd_t_dot (ccsd_t_dot.F:20-138).  Same loop order and per-element
+ * arithmetic; the two sums are Neumaier-compensated.  The reference sums
+ * with an OpenMP reduction, whose order is unspecified, so the oracle removes
+ * the order-dependent rounding instead of picking one order.
  * ==================================================================== */
+typedef struct { double s, c; } comp_t;
+static void comp_add(comp_t *a, double x) {
+    double t = a->s + x;
+    if (fabs(a->s) >= fabs(x)) a->c += (a->s - t) + x;
+    else a->c += (x - t) + a->s;
+    a->s = t;
+}
+
 void orc_ccsd_t_dot(const double *a_singles, const double *a_doubles,
                     I restricted, I h1b, I h2b, I h3b, I p4b, I p5b, I p6b,
                     const double *o_h1, const double *o_h2, const double *o_h3,
@@ -892,7 +903,7 @@ void orc_ccsd_t_dot(const double *a_singles, const double *a_doubles,
     else if (p4b == p5b || p5b == p6b) factor = factor / 2.0;
     if (h1b == h2b && h2b == h3b) factor = factor / 6.0;
     else if (h1b == h2b || h2b == h3b) factor = factor / 2.0;
-    double e1 = *energy1, e2 = *energy2;
+    comp_t e1 = {*energy1, 0.0}, e2 = {*energy2, 0.0};
     for (I p4 = 0; p4 < r_p4; p4++)
     for (I p5 = 0; p5 < r_p5; p5++)
     for (I p6 = 0; p6 < r_p6; p6++) {
@@ -908,14 +919,14 @@ void orc_ccsd_t_dot(const double *a_singles, const double *a_doubles,
                     double sing = a_singles[x];
                     double doub = a_doubles[x];
                     double denom = doub * factor / (d_h1 + d_h2 + d_h3 + denom_0);
-                    e1 = e1 + denom * doub;
-                    e2 = e2 + denom * (doub + sing);
+                    comp_add(&e1, denom * doub);
+                    comp_add(&e2, denom * (doub + sing));
                 }
             }
         }
     }
-    *energy1 = e1;
-    *energy2 = e2;
+    *energy1 = e1.s + e1.c;
+    *energy2 = e2.s + e2.c;
 }
 
 /* ======================================================================
@@ -1037,7 +1048,7 @@ I orc_ccsd_t(const orc_tiling *t, const orc_file *t1f, const orc_file *t2f,
     double *singles = (double *)malloc(sizeof(double) * maxsize);
     double *doubles = (double *)malloc(sizeof(double) * maxsize);
     if (!singles || !doubles) { free(singles); free(doubles); return -2; }
-    double e1 = 0.0, e2 = 0.0;
+    comp_t e1 = {0.0, 0.0}, e2 = {0.0, 0.0};
     for (I q = 0; q < n; q++) {
         I id = task_ids ? task_ids[q] : q;
         const I *tp = klist + 7 * id;
@@ -1057,8 +1068,8 @@ I orc_ccsd_t(const orc_tiling *t, const orc_file *t1f, const orc_file *t2f,
                        ev + t->offset[t_p5b - 1], ev + t->offset[t_p6b - 1],
                        RNG(t_h1b), RNG(t_h2b), RNG(t_h3b), RNG(t_p4b),
                        RNG(t_p5b), RNG(t_p6b), &te1, &te2);
-        e1 += te1;
-        e2 += te2;
+        comp_add(&e1, te1);
+        comp_add(&e2, te2);
         if (per_task) { per_task[2 * q] = te1; per_task[2 * q + 1] = te2; }
         if (kernel_calls) {
             kernel_calls[3 * q] = c3[0];
@@ -1068,7 +1079,7 @@ I orc_ccsd_t(const orc_tiling *t, const orc_file *t1f, const orc_file *t2f,
     }
     free(singles);
     free(doubles);
-    energy[0] = e1;
-    energy[1] = e2;
+    energy[0] = e1.s + e1.c;
+    energy[1] = e2.s + e2.c;
     return 0;
 }
