@@ -278,13 +278,15 @@ def ours(args) -> None:
 
 
 def profile_case(args) -> None:
-    """Small case for ncu: o40v300 inputs, the fused kernel on `--tuples`
-    tuples from the middle of the list, one warm-up launch then one launch."""
+    """Small case for ncu (under 1 GB on the device, operands still larger
+    than L2): o=40 as 8/12/20, v=114 as 20,24,30,40, seed 1; the fused
+    kernel on `--tuples` tuples from the middle of the weight-ordered list,
+    one warm-up launch then one launch."""
     import torch
 
     import nwchem_gb300 as ng
     torch.cuda.set_device(0)
-    t = ng.config_tiling(1)
+    t = ng.Tiling([8, 12, 20], [20, 24, 30, 40], name="o40v114").with_evl(SEED)
     kl = ng.task_list(t)
     files = ng.synth_inputs(t, SEED)
     mid = len(kl) // 2
@@ -295,7 +297,9 @@ def profile_case(args) -> None:
         job.run(sel)
         e = job.run(sel)
         print(json.dumps({"profile_case": True, "tuples": int(len(sel)), "flops": ng.flops(t, sel),
-                          "kernel_ms": job.last_kernel_ms, "energies": list(e)}), flush=True)
+                          "kernel_ms": job.last_kernel_ms, "device_bytes": job.device_bytes,
+                          "tflops": ng.flops(t, sel) / job.last_kernel_ms / 1e9, "energies": list(e)}),
+              flush=True)
 
 
 def main() -> None:

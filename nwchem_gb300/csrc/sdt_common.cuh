@@ -38,10 +38,12 @@ cudaStream_t lib_stream();
 // Returns SDT_OK or records a CUDA error with context.
 int cuda_check(cudaError_t e, const char *what);
 
-// Caching allocator (device and pinned host), memory.cu semantics.
-void *gpu_get(size_t bytes);
+// Caching allocator (device and pinned host), memory.cu semantics.  Blocks
+// taken with tile = true belong to the reference tile ABI and are the ones
+// finalizememmodule_ requires to be released.
+void *gpu_get(size_t bytes, bool tile = false);
 void gpu_put(void *p);
-void *host_get(size_t bytes);
+void *host_get(size_t bytes, bool tile = false);
 void host_put(void *p);
 
 // Reduction of per-block (E[T], E(T)) partials: out[2] on the device.

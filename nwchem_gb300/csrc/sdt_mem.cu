@@ -17,6 +17,7 @@ namespace {
 struct Pool {
     std::multimap<size_t, void *> free_dev, free_host;
     std::map<void *, size_t> live_dev, live_host;
+    std::map<void *, bool> tile_owned;  // live blocks of the tile ABI
     bool init = false;
 };
 Pool &pool() {
@@ -75,27 +76,33 @@ static void *take(std::multimap<size_t, void *> &fl, std::map<void *, size_t> &l
     return p;
 }
 
-void *gpu_get(size_t bytes) {
+void *gpu_get(size_t bytes, bool tile) {
     std::lock_guard<std::mutex> lk(pool_mu());
     if (bytes == 0) bytes = 8;
-    return take(pool().free_dev, pool().live_dev, bytes, true);
+    void *p = take(pool().free_dev, pool().live_dev, bytes, true);
+    if (p && tile) pool().tile_owned[p] = true;
+    return p;
 }
 void gpu_put(void *p) {
     if (!p) return;
     std::lock_guard<std::mutex> lk(pool_mu());
+    pool().tile_owned.erase(p);
     auto it = pool().live_dev.find(p);
     if (it == pool().live_dev.end()) return;
     pool().free_dev.emplace(it->second, p);
     pool().live_dev.erase(it);
 }
-void *host_get(size_t bytes) {
+void *host_get(size_t bytes, bool tile) {
     std::lock_guard<std::mutex> lk(pool_mu());
     if (bytes == 0) bytes = 8;
-    return take(pool().free_host, pool().live_host, bytes, false);
+    void *p = take(pool().free_host, pool().live_host, bytes, false);
+    if (p && tile) pool().tile_owned[p] = true;
+    return p;
 }
 void host_put(void *p) {
     if (!p) return;
     std::lock_guard<std::mutex> lk(pool_mu());
+    pool().tile_owned.erase(p);
     auto it = pool().live_host.find(p);
     if (it == pool().live_host.end()) return;
     pool().free_host.emplace(it->second, p);
@@ -161,7 +168,7 @@ extern "C" void finalizememmodule_(void) {
     bool leaked;
     {
         std::lock_guard<std::mutex> lk(pool_mu());
-        leaked = !pool().live_host.empty() || !pool().live_dev.empty();
+        leaked = !pool().tile_owned.empty();
         pool().init = false;
         // Freed blocks stay cached for the next tuple; memory.cu returns them
         // to the driver here, which costs a cudaFree/cudaMalloc per tuple.

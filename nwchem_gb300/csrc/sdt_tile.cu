@@ -234,7 +234,7 @@ bool ensure(double **buf, size_t *cap, size_t n) {
         gpu_put(*buf);
     }
     size_t want = n < 4096 ? 4096 : n + n / 4;
-    *buf = (double *)gpu_get(want * sizeof(double));
+    *buf = (double *)gpu_get(want * sizeof(double), true);
     *cap = *buf ? want : 0;
     return *buf != nullptr;
 }
@@ -255,7 +255,7 @@ int alloc_tile(double **t, int64_t *n, int64_t size, const char *what) {
         gpu_put(*t);
         *t = nullptr;
     }
-    *t = (double *)gpu_get((size_t)size * sizeof(double));
+    *t = (double *)gpu_get((size_t)size * sizeof(double), true);
     if (!*t) return fail(SDT_ERR_NOMEM, std::string(what) + ": device allocation");
     *n = size;
     return cuda_check(cudaMemsetAsync(*t, 0, (size_t)size * sizeof(double), st), what);
@@ -423,19 +423,27 @@ extern "C" void compute_en_(double *factor, double *energy, double *eval1, doubl
         return;
     }
     cudaStream_t st = lib_stream();
-    if (!g_tile.ebuf) {
-        g_tile.ebuf = (double *)gpu_get(6 * 4096 * sizeof(double));
-        g_tile.epart = (double *)gpu_get(2 * kEnergyBlocks * sizeof(double));
-        g_tile.eout = (double *)gpu_get(2 * sizeof(double));
-        g_tile.ehost = (double *)host_get(8 * 4096 * sizeof(double));
-        if (!g_tile.ebuf || !g_tile.epart || !g_tile.eout || !g_tile.ehost) {
-            ok_or_abort(fail(SDT_ERR_NOMEM, "compute_en_: allocation"));
-            return;
+    // Per-call buffers (memory.cu-style: taken and given back every call;
+    // the cache makes the second call allocation-free).
+    g_tile.ebuf = (double *)gpu_get(6 * 4096 * sizeof(double), true);
+    g_tile.epart = (double *)gpu_get(2 * kEnergyBlocks * sizeof(double), true);
+    g_tile.eout = (double *)gpu_get(2 * sizeof(double), true);
+    g_tile.ehost = (double *)host_get(8 * 4096 * sizeof(double), true);
+    struct Release {
+        ~Release() {
+            gpu_put(g_tile.ebuf);
+            gpu_put(g_tile.epart);
+            gpu_put(g_tile.eout);
+            host_put(g_tile.ehost);
+            g_tile.ebuf = g_tile.epart = g_tile.eout = g_tile.ehost = nullptr;
         }
+    } release;
+    if (!g_tile.ebuf || !g_tile.epart || !g_tile.eout || !g_tile.ehost) {
+        ok_or_abort(fail(SDT_ERR_NOMEM, "compute_en_: allocation"));
+        return;
     }
     double *ev[6] = {eval1, eval2, eval3, eval4, eval5, eval6};
     int64_t at = 0;
-    cudaStreamSynchronize(st);  // ehost may still be the source of a prior copy
     for (int q = 0; q < 6; ++q) {
         if (d[q] > 4096) {
             ok_or_abort(fail(SDT_ERR_ARG, "compute_en_: tile longer than 4096"));

@@ -125,16 +125,21 @@ def test_tuples_through_tile_abi_match_oracle(lib, occ, vir, osym, vsym):
     t = ng.Tiling(occ, vir, occ_sym=osym, vir_sym=vsym).with_evl(8)
     P = orc.Problem(t, *ng.synth_inputs(t, 8))
     kl = P.task_list()
-    _, _, per_task, _ = P.ccsd_t()
+    e_tot, _, per_task, _ = P.ccsd_t()
+    tiles = [P.tuple_tiles([int(x) for x in kl[q, :6]]) for q in range(len(kl))]
+    # Tolerances scale with the problem, not the tuple: some tuples are exactly
+    # zero by antisymmetry (three holes in a two-orbital tile) and come out
+    # as +-1e-18 rounding on either side.
+    sd = max(np.abs(rd).max() for _, rd in tiles)
+    ss = max(np.abs(rs).max() for rs, _ in tiles)
     for q in range(len(kl)):
         tup = [int(x) for x in kl[q, :6]]
         e, d, s, _ = _drive_tuple(lib, P, t, tup)
-        rs, rd = P.tuple_tiles(tup)
-        sc = max(np.abs(rd).max(), 1e-300)
-        assert np.abs(d - rd.ravel(order="F")).max() <= 1e-13 * sc
-        assert np.abs(s - rs.ravel(order="F")).max() <= 1e-13 * max(np.abs(rs).max(), 1e-300)
-        assert e[0] == pytest.approx(per_task[q, 0], rel=1e-12, abs=1e-300)
-        assert e[1] == pytest.approx(per_task[q, 1], rel=1e-12, abs=1e-300)
+        rs, rd = tiles[q]
+        assert np.abs(d - rd.ravel(order="F")).max() <= 1e-13 * sd
+        assert np.abs(s - rs.ravel(order="F")).max() <= 1e-13 * ss
+        assert e[0] == pytest.approx(per_task[q, 0], rel=1e-12, abs=1e-13 * abs(e_tot))
+        assert e[1] == pytest.approx(per_task[q, 1], rel=1e-12, abs=1e-13 * abs(e_tot))
     lib.dev_release_()
     assert _capi.last_error()[0] == 0
 
@@ -146,3 +151,22 @@ def test_tile_abi_rejects_mismatched_dims(lib):
     code, msg = _capi.last_error()
     assert code == 1 and "do not match" in msg
     lib.dev_release_()
+
+
+def test_memory_module_checks_live_blocks(lib):
+    """finalizememmodule_ accepts a released tuple and flags a leaked one
+    (memory.cu:164-171 asserts no live pointers)."""
+    dims = _refs((2, 2, 2, 3, 3, 3))
+    lib.initmemmodule_()
+    lib.dev_mem_d_(*dims)
+    lib.dev_mem_s_(*dims)
+    lib.dev_release_()
+    lib.finalizememmodule_()
+    assert _capi.last_error()[0] == 0
+    lib.initmemmodule_()
+    lib.dev_mem_d_(*dims)
+    lib.finalizememmodule_()
+    code, msg = _capi.last_error()
+    assert code == 4 and "live" in msg
+    lib.dev_release_()
+    lib.initmemmodule_()
