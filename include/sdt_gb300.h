@@ -83,6 +83,32 @@ void dev_mem_d_(sdt_int *h1d, sdt_int *h2d, sdt_int *h3d, sdt_int *p4d,
                 sdt_int *p5d, sdt_int *p6d);
 void dev_mem_s_(sdt_int *h1d, sdt_int *h2d, sdt_int *h3d, sdt_int *p4d,
                 sdt_int *p5d, sdt_int *p6d);
+/* Energy of triples tiles that the CALLER owns in device memory, without any
+ * device allocation.  No counterpart in the reference.  It is for callers
+ * that keep t3 (and t3_s) in device memory they manage themselves -- their
+ * own pool, or arrays owned by a Fortran offload runtime -- and cannot or
+ * must not call cudaMalloc/cudaFree (their pool holds the memory budget, or
+ * an allocation would synchronise the device under their running work).
+ * Arguments and results are compute_en_'s: host orbital energies
+ * eval1..eval6 (h1,h2,h3,p4,p5,p6), tile lengths, factor, and energy[0] =
+ * E[T], energy[1] = E(T) on the host; t3_d / t3s_d are the tuple-layout
+ * (h3,h2,h1,p6,p5,p4) device tiles (t3s_d may be NULL: no singles).
+ * Its scratch is one fixed __device__ array (about 82 KB on every GPU that
+ * loads the library, held until exit): h1d+h2d+h3d+p4d+p5d+p6d may not
+ * exceed 8192, larger requests fail with SDT_ERR_ARG.  The first call on a
+ * device looks up that array's device address (cudaGetSymbolAddress) with
+ * the device current; make that first call before any stream capture.
+ * All calls share the array, so calls that overlap on the GPU race; every
+ * scratch element a call reads is written earlier in the same call.
+ * Work is queued on `stream` (NULL: the legacy default stream) and the
+ * call returns after synchronising it. */
+int sdt_compute_en_noalloc(double factor, double *energy, const double *eval1,
+                           const double *eval2, const double *eval3,
+                           const double *eval4, const double *eval5,
+                           const double *eval6, int64_t h1d, int64_t h2d,
+                           int64_t h3d, int64_t p4d, int64_t p5d,
+                           int64_t p6d, const double *t3_d,
+                           const double *t3s_d, void *stream);
 /* Copies the current device tiles to host buffers of the tuple size (either
  * may be NULL).  No reference counterpart: the reference only exposes the
  * tiles through compute_en_; this read-back exists for parity tests. */

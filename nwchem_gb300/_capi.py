@@ -62,6 +62,8 @@ def _declare(lib):
         "dev_mem_s_": (None, [PI64] * 6),
         "dev_release_": (None, []),
         "sdt_tile_download": (C.c_int, [PD, PD]),
+        "sdt_compute_en_noalloc": (C.c_int, [C.c_double, PD, PD, PD, PD, PD, PD, PD, I64, I64, I64, I64, I64,
+                                             I64, C.c_void_p, C.c_void_p, C.c_void_p]),
         "initmemmodule_": (None, []),
         "finalizememmodule_": (None, []),
         "check_device_": (C.c_int, [C.POINTER(C.c_long)]),
