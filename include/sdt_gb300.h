@@ -192,7 +192,11 @@ int sdt_synth_evl(int64_t nocc, int64_t nvir, uint64_t seed, double *evl);
 
 /* A job holds one (T) problem resident on the device. */
 typedef struct sdt_job sdt_job;
-enum { SDT_PREC_FP64 = 0 };
+/* Precision of sdt_job_run: FP64 throughout, or the mixed form (d1/d2
+ * contractions as TF32 split products hi*hi + hi*lo + lo*hi with FP32
+ * accumulation on the tensor cores; triples promoted to FP64 before the
+ * s1 terms, the denominator and the energy sums). */
+enum { SDT_PREC_FP64 = 0, SDT_PREC_MIXED_TF32 = 1 };
 int sdt_job_create(const sdt_tiling *t, sdt_job **job);
 /* Copy the host TCE files to the device and re-lay them out for the fused
  * kernel (antisymmetric mirrors, signs of tce_hashnsort.F).  Device-side
@@ -229,6 +233,15 @@ int64_t sdt_launch_count(void);
  * SMs for about `ms` milliseconds.  The roofline denominator of the FP64
  * form. */
 double sdt_probe_fp64_tflops(int ms);
+
+/* Self-test of the tensor-core path of the mixed form (no reference
+ * counterpart): D[128][256] = A*B^T on one SM with A = a_hi + a_lo
+ * ([128][K]) and B = b_hi + b_lo ([256][K]) given as TF32 values in fp32
+ * device arrays, K a multiple of 4, the three split products accumulated in
+ * FP32 by tcgen05.mma from TMA-staged shared memory.  D is a device array.
+ * SDT_ERR_TIMEOUT if a bounded wait in the kernel ran out. */
+int sdt_tc_selftest(const float *a_hi, const float *a_lo, const float *b_hi,
+                    const float *b_lo, int K, float *D);
 
 #ifdef __cplusplus
 }

@@ -25,6 +25,7 @@
 //        +t1(ci)u(abjk) -t1(cj)u(abik) +t1(ck)u(abij)
 // (row k of each block is kernel k of its family, in order).
 #include "sdt_common.cuh"
+#include "sdt_job.h"
 
 #include <algorithm>
 #include <cstring>
@@ -53,8 +54,6 @@ struct CopyJob {
     int32_t src_file;     // 0 T1, 1 T2, 2 V2
     int32_t dst_array;    // index into the destination table
 };
-
-enum { DST_T1 = 0, DST_T2A, DST_T2B, DST_VD2, DST_WD1, DST_UD, DST_N };
 
 struct IngestArgs {
     const double *src[3];
@@ -366,33 +365,19 @@ __global__ void __launch_bounds__(256) tuple_sum_kernel(const double *__restrict
 }
 
 }  // namespace
+
+int finish_run(sdt_job *j, int64_t n, cudaStream_t st) {
+    for (int64_t q0 = 0; q0 < n; q0 += 65535) {
+        const unsigned nb = (unsigned)std::min<int64_t>(65535, n - q0);
+        tuple_sum_kernel<<<nb, 256, 0, st>>>(j->part_d, j->pref_d + q0, nb, j->task_d + 2 * q0);
+        count_launch();
+    }
+    return reduce_pairs(j->task_d, n, j->out_d, st);
+}
+
 }  // namespace sdt
 
 using namespace sdt;
-
-struct sdt_job {
-    Tiling t;
-    std::vector<int64_t> range, spin, sym, offset, alpha;
-    std::vector<double> evl;
-    int dev = 0;
-    // device
-    int32_t *tiles = nullptr;
-    double *evl_d = nullptr;
-    int64_t *pair_off = nullptr;
-    double *arr[DST_N] = {nullptr};
-    size_t arr_n[DST_N] = {0};
-    bool loaded = false;
-    // run workspace
-    int64_t *klist_d = nullptr, *pref_d = nullptr;
-    double *factor_d = nullptr, *part_d = nullptr, *task_d = nullptr, *out_d = nullptr;
-    size_t cap_tasks = 0, cap_items = 0;
-    double *host_out = nullptr;
-    size_t cap_host = 0;
-    // optional CUDA-event timing of the fused launches of the last run
-    bool timing = false;
-    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-    float last_ms = 0.0f;
-};
 
 namespace {
 
@@ -498,7 +483,9 @@ extern "C" int sdt_job_load(sdt_job *j, const sdt_file *f1, const sdt_file *f2,
     const size_t want[DST_N] = {(size_t)(v * o), (size_t)(v * v * o * o), (size_t)(v * v * o * o),
                                 (size_t)vd2, (size_t)(v * o * o * o), (size_t)(v * v * o * o)};
     job_free_arrays(j);
+    mixed_release(j);
     j->loaded = false;
+    j->pair_host = pair;
     for (int a = 0; a < DST_N; ++a) {
         j->arr[a] = (double *)gpu_get(want[a] * sizeof(double));
         if (!j->arr[a]) {
@@ -693,7 +680,11 @@ extern "C" int sdt_job_run(sdt_job *j, const int64_t *klist, int64_t n, int prec
                            double *energy, double *per_task, void *stream) {
     if (!j || !energy || (n > 0 && !klist)) return fail(SDT_ERR_ARG, "sdt_job_run: null argument");
     if (!j->loaded) return fail(SDT_ERR_STATE, "sdt_job_run: sdt_job_load has not succeeded");
-    if (precision != SDT_PREC_FP64) return fail(SDT_ERR_ARG, "sdt_job_run: unknown precision");
+    if (precision != SDT_PREC_FP64 && precision != SDT_PREC_MIXED_TF32)
+        return fail(SDT_ERR_ARG, "sdt_job_run: unknown precision");
+    const bool mixed = precision == SDT_PREC_MIXED_TF32;
+    // Sub-box edges: 4 in every index (FP64); 8 virtual x 4 occupied (mixed).
+    const int box_v = mixed ? 8 : BOX, box_o = BOX;
     energy[0] = energy[1] = 0.0;
     if (n == 0) return SDT_OK;
     cudaStream_t st = stream ? (cudaStream_t)stream : lib_stream();
@@ -708,7 +699,8 @@ extern "C" int sdt_job_run(sdt_job *j, const int64_t *klist, int64_t n, int prec
             const bool virt = d < 3;
             if (k[d] < 1 || k[d] > nt || (virt ? k[d] <= t.noab : k[d] > t.noab))
                 return fail(SDT_ERR_ARG, "sdt_job_run: tuple tile out of range");
-            boxes *= (t.r(k[d]) + BOX - 1) / BOX;
+            const int bx = virt ? box_v : box_o;
+            boxes *= (t.r(k[d]) + bx - 1) / bx;
         }
         if (!(k[0] <= k[1] && k[1] <= k[2] && k[3] <= k[4] && k[4] <= k[5]))
             return fail(SDT_ERR_ARG, "sdt_job_run: tuple tiles not sorted");
@@ -750,6 +742,20 @@ extern "C" int sdt_job_run(sdt_job *j, const int64_t *klist, int64_t n, int prec
     if (!rc) rc = cuda_check(cudaMemcpyAsync(j->factor_d, fac.data(), n * sizeof(double), cudaMemcpyHostToDevice, st), "sdt_job_run");
     if (rc) return rc;
 
+    if (mixed) {
+        if (!j->mixed_ready) {
+            rc = mixed_prepare(j, st);
+            if (rc) return rc;
+        }
+        if (j->timing) {
+            if (!j->ev0) cudaEventCreate(&j->ev0);
+            if (!j->ev1) cudaEventCreate(&j->ev1);
+            cudaEventRecord(j->ev0, st);
+        }
+        rc = mixed_launch(j, items, n, st);
+        if (j->timing) cudaEventRecord(j->ev1, st);
+        if (rc) return rc;
+    } else {
     FusedParams p;
     p.T1d = j->arr[DST_T1]; p.T2a = j->arr[DST_T2A]; p.T2b = j->arr[DST_T2B];
     p.Vd2 = j->arr[DST_VD2]; p.Wd1 = j->arr[DST_WD1]; p.Ud = j->arr[DST_UD];
@@ -776,12 +782,8 @@ extern "C" int sdt_job_run(sdt_job *j, const int64_t *klist, int64_t n, int prec
     if (j->timing) cudaEventRecord(j->ev1, st);
     rc = cuda_check(cudaGetLastError(), "sdt_job_run: fused kernel");
     if (rc) return rc;
-    for (int64_t q0 = 0; q0 < n; q0 += 65535) {
-        const unsigned nb = (unsigned)std::min<int64_t>(65535, n - q0);
-        tuple_sum_kernel<<<nb, 256, 0, st>>>(j->part_d, j->pref_d + q0, nb, j->task_d + 2 * q0);
-        count_launch();
     }
-    rc = reduce_pairs(j->task_d, n, j->out_d, st);
+    rc = finish_run(j, n, st);
     if (rc) return rc;
     rc = cuda_check(cudaMemcpyAsync(j->host_out, j->out_d, 2 * sizeof(double), cudaMemcpyDeviceToHost, st), "sdt_job_run");
     if (!rc && per_task)
@@ -790,6 +792,9 @@ extern "C" int sdt_job_run(sdt_job *j, const int64_t *klist, int64_t n, int prec
     rc = cuda_check(cudaStreamSynchronize(st), "sdt_job_run");
     if (rc) return rc;
     if (j->timing) cudaEventElapsedTime(&j->last_ms, j->ev0, j->ev1);
+    if (mixed && j->err_h && *j->err_h)
+        return fail(SDT_ERR_TIMEOUT, "sdt_job_run: a bounded wait in the mixed kernel ran out (code " +
+                                         std::to_string(*j->err_h) + ")");
     energy[0] = j->host_out[0];
     energy[1] = j->host_out[1];
     if (per_task) std::memcpy(per_task, j->host_out + 2, 2 * n * sizeof(double));
@@ -800,6 +805,7 @@ extern "C" int sdt_job_destroy(sdt_job *j) {
     if (!j) return SDT_OK;
     cudaStreamSynchronize(lib_stream());
     job_free_arrays(j);
+    mixed_release(j);
     gpu_put(j->tiles);
     gpu_put(j->evl_d);
     gpu_put(j->pair_off);

@@ -1,0 +1,62 @@
+// sdt_job.h -- the batched job object shared by the FP64 and mixed paths.
+#pragma once
+#include <cuda.h>
+#include <cuda_runtime.h>
+#include <vector>
+#include "sdt_internal.h"
+
+namespace sdt {
+enum { DST_T1 = 0, DST_T2A, DST_T2B, DST_VD2, DST_WD1, DST_UD, DST_N };
+// TF32 hi/lo copies of the contraction operands (mixed form).
+enum { SP_T2A = 0, SP_T2B, SP_WD1, SP_VD2, SP_N };
+}  // namespace sdt
+
+struct sdt_job {
+    using Tiling = sdt::Tiling;
+    Tiling t;
+    std::vector<int64_t> range, spin, sym, offset, alpha;
+    std::vector<double> evl;
+    int dev = 0;
+    // device
+    int32_t *tiles = nullptr;
+    double *evl_d = nullptr;
+    int64_t *pair_off = nullptr;
+    double *arr[sdt::DST_N] = {nullptr};
+    size_t arr_n[sdt::DST_N] = {0};
+    std::vector<int64_t> pair_host;     // Vd2 region offsets (fp64 elements), -1 if none
+    // mixed form: split operands (hi at [2*k], lo at [2*k+1]) and tensor maps
+    float *sp[2 * sdt::SP_N] = {nullptr};
+    size_t sp_n[2 * sdt::SP_N] = {0};
+    int64_t o_pad = 0, v_pad = 0;
+    bool mixed_ready = false;
+    CUtensorMap maps[6];                 // t2b hi/lo, t2a hi/lo, wd1 hi/lo
+    CUtensorMap *vd2_maps = nullptr;     // device: 2 per virtual tile pair
+    int32_t *pair_id = nullptr;          // device: [nvab*nvab] -> pair index or -1
+    int *err_d = nullptr;
+    int *err_h = nullptr;                // pinned copy of err_d
+    bool loaded = false;
+    // run workspace
+    int64_t *klist_d = nullptr, *pref_d = nullptr;
+    double *factor_d = nullptr, *part_d = nullptr, *task_d = nullptr, *out_d = nullptr;
+    size_t cap_tasks = 0, cap_items = 0;
+    double *host_out = nullptr;
+    size_t cap_host = 0;
+    // optional CUDA-event timing of the fused launches of the last run
+    bool timing = false;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    float last_ms = 0.0f;
+};
+
+
+namespace sdt {
+// Per-tuple compensated sums of the item partials, the total, into out_d.
+int finish_run(sdt_job *j, int64_t n, cudaStream_t st);
+// Frees the mixed-form operands and maps of a job.
+void mixed_release(sdt_job *j);
+// Builds the split operands and tensor maps (after a successful load).
+int mixed_prepare(sdt_job *j, cudaStream_t st);
+// Launches the mixed fused kernel over the prepared items.
+int mixed_launch(sdt_job *j, int64_t items, int64_t n, cudaStream_t st);
+int make_tmap_f32(CUtensorMap *map, const void *base, int rank, const uint64_t *dims,
+                  const uint64_t *strides_bytes, const uint32_t *box);
+}  // namespace sdt

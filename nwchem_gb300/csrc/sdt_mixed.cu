@@ -1,0 +1,728 @@
+// sdt_mixed.cu -- the mixed-precision form on 5th-generation tensor cores.
+//
+// Split products: every FP64 operand x is stored as two TF32 values
+// hi = tf32(x), lo = tf32(x - hi) (fp32 containers), and a product is taken
+// as hi*hi + hi*lo + lo*hi with FP32 accumulation in tensor memory
+// (tcgen05.mma kind::tf32).  The residual lo*lo and the split error are
+// ~2^-22 of |x*y|.
+//
+// This file holds the building blocks and a self-test GEMM that checks
+// them: TMA loads of 64-byte-swizzled K-major tiles, the shared-memory and
+// instruction descriptors, TMEM allocation, MMA issue/commit and TMEM
+// loads, with every mbarrier wait bounded in time (an error flag is set and
+// the kernel drains and returns instead of spinning forever).
+#include "sdt_common.cuh"
+#include "sdt_job.h"
+#include "sdt_tc.cuh"
+
+#include <algorithm>
+#include <vector>
+
+#include <cuda.h>
+#include <mutex>
+
+namespace sdt {
+
+// cuTensorMapEncodeTiled through the runtime's driver entry point (the
+// library does not link libcuda directly).
+typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *,
+                                  const cuuint64_t *, const cuuint64_t *, const cuuint32_t *,
+                                  const cuuint32_t *, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                  CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiledFn encode_tiled() {
+    static std::once_flag once;
+    static EncodeTiledFn fn = nullptr;
+    std::call_once(once, [] {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = (EncodeTiledFn)p;
+        else
+            cudaGetLastError();
+    });
+    return fn;
+}
+
+// fp32 tensor map with 64-byte swizzle; dims innermost first, strides in
+// bytes for dims 1..rank-1.
+int make_tmap_f32(CUtensorMap *map, const void *base, int rank, const uint64_t *dims,
+                  const uint64_t *strides_bytes, const uint32_t *box) {
+    EncodeTiledFn fn = encode_tiled();
+    if (!fn) return fail(SDT_ERR_CUDA, "cuTensorMapEncodeTiled is unavailable");
+    if ((reinterpret_cast<uintptr_t>(base) & 15) != 0) return fail(SDT_ERR_ARG, "tensor map base not 16-byte aligned");
+    cuuint64_t gd[5], gs[4];
+    cuuint32_t bx[5], es[5];
+    for (int i = 0; i < rank; ++i) {
+        gd[i] = dims[i];
+        bx[i] = box[i];
+        es[i] = 1;
+        if (i > 0) {
+            if (strides_bytes[i - 1] % 16) return fail(SDT_ERR_ARG, "tensor map stride not a multiple of 16 bytes");
+            gs[i - 1] = strides_bytes[i - 1];
+        }
+    }
+    if (box[0] * 4 > 64) return fail(SDT_ERR_ARG, "64-byte swizzle needs an inner box of at most 16 fp32");
+    CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, rank, const_cast<void *>(base), gd, gs, bx, es,
+                    CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B,
+                    CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return fail(SDT_ERR_CUDA, "cuTensorMapEncodeTiled failed (" + std::to_string((int)r) + ")");
+    return SDT_OK;
+}
+
+namespace {
+
+constexpr uint64_t kWaitNs = 2000000000ull;  // 2 s per wait
+constexpr int KC = 16;                       // fp32 K elements per stage (64 B rows)
+constexpr int ST_M = 128, ST_N = 256;
+constexpr int A_BYTES = ST_M * KC * 4;       // 8 KB
+constexpr int B_BYTES = ST_N * KC * 4;       // 16 KB
+constexpr int STAGE_BYTES = 2 * A_BYTES + 2 * B_BYTES;
+
+struct SelfTestArgs {
+    CUtensorMap a_hi, a_lo, b_hi, b_lo;  // [M=128][K], [N=256][K]
+    int K;
+    float *D;   // [128][256]
+    int *err;
+};
+
+// One CTA, 6 warps: 0 TMA producer, 1 MMA issuer + TMEM owner, 2-5 epilogue.
+__global__ void __launch_bounds__(192, 1) tc_selftest_kernel(const __grid_constant__ SelfTestArgs g) {
+    extern __shared__ __align__(1024) uint8_t smem_raw[];
+    uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    uint64_t *full = (uint64_t *)(smem + 2 * STAGE_BYTES);
+    uint64_t *empty = full + 2;
+    uint64_t *tfull = empty + 2;
+    uint32_t *tslot = (uint32_t *)(tfull + 1);
+    volatile int *abort = (volatile int *)(tslot + 1);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int nk = (g.K + KC - 1) / KC;
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < 2; ++s) {
+            tc::mbar_init(&full[s], 1);
+            tc::mbar_init(&empty[s], 1);
+        }
+        tc::mbar_init(tfull, 1);
+        *abort = 0;
+        tc::fence_mbar_init();
+    }
+    if (warp == 1) tc::tmem_alloc(tslot, 256);
+    tc::tc_fence_before();
+    __syncthreads();
+    tc::tc_fence_after();
+    const uint32_t tmem = *tslot;
+
+    if (warp == 0 && lane == 0) {
+        tc::prefetch_tmap(&g.a_hi);
+        tc::prefetch_tmap(&g.b_hi);
+        for (int kc = 0; kc < nk && !*abort; ++kc) {
+            const int s = kc & 1;
+            if (kc >= 2 && !tc::mbar_wait(&empty[s], ((kc >> 1) & 1) ^ 1, kWaitNs, abort)) {
+                *abort = 1;
+                atomicExch(g.err, 1);
+                break;
+            }
+            uint8_t *st = smem + s * STAGE_BYTES;
+            tc::mbar_arrive_expect_tx(&full[s], STAGE_BYTES);
+            tc::tma_load_2d(st, &g.a_hi, &full[s], kc * KC, 0);
+            tc::tma_load_2d(st + A_BYTES, &g.a_lo, &full[s], kc * KC, 0);
+            tc::tma_load_2d(st + 2 * A_BYTES, &g.b_hi, &full[s], kc * KC, 0);
+            tc::tma_load_2d(st + 2 * A_BYTES + B_BYTES, &g.b_lo, &full[s], kc * KC, 0);
+        }
+    } else if (warp == 1 && lane == 0) {
+        const uint32_t idesc = tc::idesc_tf32(ST_M, ST_N);
+        for (int kc = 0; kc < nk; ++kc) {
+            const int s = kc & 1;
+            if (!tc::mbar_wait(&full[s], (kc >> 1) & 1, kWaitNs, abort)) {
+                *abort = 1;
+                atomicExch(g.err, 2);
+                break;
+            }
+            tc::tc_fence_after();
+            const uint32_t st = tc::smem_u32(smem + s * STAGE_BYTES);
+            for (int kk = 0; kk < KC / 8; ++kk) {
+                const uint32_t ah = st + kk * 32, al = st + A_BYTES + kk * 32;
+                const uint32_t bh = st + 2 * A_BYTES + kk * 32, bl = st + 2 * A_BYTES + B_BYTES + kk * 32;
+                const uint32_t first = (kc == 0 && kk == 0) ? 0u : 1u;
+                tc::mma_tf32(tmem, tc::sdesc_sw64(ah), tc::sdesc_sw64(bh), idesc, first);
+                tc::mma_tf32(tmem, tc::sdesc_sw64(ah), tc::sdesc_sw64(bl), idesc, 1u);
+                tc::mma_tf32(tmem, tc::sdesc_sw64(al), tc::sdesc_sw64(bh), idesc, 1u);
+            }
+            tc::mma_commit(&empty[s]);
+        }
+        tc::mma_commit(tfull);
+    } else if (warp >= 2) {
+        const int quad = warp & 3;  // TMEM lanes 32*quad .. 32*quad+31
+        if (tc::mbar_wait(tfull, 0, kWaitNs, abort)) {
+            tc::tc_fence_after();
+            const int row = quad * 32 + lane;
+            for (int c = 0; c < ST_N / 32; ++c) {
+                float v[32];
+                tc::tmem_ld32(tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(c * 32), v);
+#pragma unroll
+                for (int q = 0; q < 32; ++q) g.D[row * ST_N + c * 32 + q] = v[q];
+            }
+        } else {
+            *abort = 1;
+            atomicExch(g.err, 3);
+        }
+    }
+    tc::tc_fence_before();
+    __syncthreads();
+    // Drain after an abort (bounded): copies in flight must land and issued
+    // MMAs must finish before the CTA frees TMEM and exits.
+    if (*abort && lane == 0 && warp <= 1) {
+        volatile int never = 0;
+        if (warp == 0)
+            for (int s = 0; s < 2; ++s)
+                for (uint32_t ph = 0; ph < 2; ++ph) tc::mbar_wait(&full[s], ph, kWaitNs / 8, &never);
+        else
+            tc::mbar_wait(tfull, 0, kWaitNs, &never);
+    }
+    __syncthreads();
+    if (warp == 1) {
+        tc::tc_fence_after();
+        tc::tmem_dealloc(tmem, 256);
+    }
+}
+
+}  // namespace
+}  // namespace sdt
+
+using namespace sdt;
+
+// D[128][256] = A*B^T with A = a_hi + a_lo ([128][K]) and B = b_hi + b_lo
+// ([256][K]) given as TF32 values in fp32 arrays; the three split products
+// are accumulated in FP32 in tensor memory.  Returns SDT_ERR_TIMEOUT when a
+// bounded wait inside the kernel ran out.
+extern "C" int sdt_tc_selftest(const float *a_hi, const float *a_lo, const float *b_hi, const float *b_lo,
+                               int K, float *D) {
+    if (K < 4 || K % 4) return fail(SDT_ERR_ARG, "sdt_tc_selftest: K must be a positive multiple of 4");
+    SelfTestArgs g;
+    const uint64_t da[2] = {(uint64_t)K, 128}, db[2] = {(uint64_t)K, 256};
+    const uint64_t sa[1] = {(uint64_t)K * 4};
+    const uint32_t ba[2] = {KC, 128}, bb[2] = {KC, 256};
+    int rc = make_tmap_f32(&g.a_hi, a_hi, 2, da, sa, ba);
+    if (!rc) rc = make_tmap_f32(&g.a_lo, a_lo, 2, da, sa, ba);
+    if (!rc) rc = make_tmap_f32(&g.b_hi, b_hi, 2, db, sa, bb);
+    if (!rc) rc = make_tmap_f32(&g.b_lo, b_lo, 2, db, sa, bb);
+    if (rc) return rc;
+    g.K = K;
+    g.D = D;
+    int *err = (int *)gpu_get(sizeof(int));
+    if (!err) return fail(SDT_ERR_NOMEM, "sdt_tc_selftest: flag");
+    g.err = err;
+    cudaStream_t st = lib_stream();
+    const int smem = 2 * STAGE_BYTES + 1024 + 256;
+    rc = cuda_check(cudaFuncSetAttribute(tc_selftest_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem),
+                    "sdt_tc_selftest");
+    if (!rc) rc = cuda_check(cudaMemsetAsync(err, 0, sizeof(int), st), "sdt_tc_selftest");
+    if (rc) {
+        gpu_put(err);
+        return rc;
+    }
+    tc_selftest_kernel<<<1, 192, smem, st>>>(g);
+    count_launch();
+    int h = 0;
+    rc = cuda_check(cudaGetLastError(), "sdt_tc_selftest");
+    if (!rc) rc = cuda_check(cudaMemcpyAsync(&h, err, sizeof(int), cudaMemcpyDeviceToHost, st), "sdt_tc_selftest");
+    if (!rc) rc = cuda_check(cudaStreamSynchronize(st), "sdt_tc_selftest");
+    gpu_put(err);
+    if (rc) return rc;
+    if (h) return fail(SDT_ERR_TIMEOUT, "sdt_tc_selftest: a bounded wait ran out (stage " + std::to_string(h) + ")");
+    return SDT_OK;
+}
+
+// ===========================================================================
+// Fused mixed-precision tuple kernel.
+//
+// One CTA (192 threads, one per SM) owns an 8x8x8 (a,b,c) x 4x4x4 (i,j,k)
+// sub-box of one tuple's triples tile: 32768 FP32 values in shared memory.
+// Each of the 18 d1/d2 terms is one 128x256xK GEMM on the tensor cores:
+//   d2: A = t(P,e;H,H')  (rows P*16+H*4+H', from T2b), B = v(Q,Q',H'',e)
+//       (cols Q*32+Q'*4+H'', from the Vd2 region of tiles (Q,Q')), K = e;
+//   d1: A = w(m,Q,H',H'') (rows Q*16+H'*4+H'', from Wd1), B = t(P,P';H,m)
+//       (cols P*32+P'*4+H, from T2a), K = m;
+// with operand tiles staged by TMA (64-byte swizzle, 16 K per stage, two
+// stages) and the three split products issued by one thread into one of two
+// TMEM accumulators (256 columns each).  Four epilogue warps drain the other
+// accumulator and add it, with the term's sign, into the sub-box.  The
+// epilogue then promotes to FP64, adds the s1 products and the denominator
+// and writes the CTA's (E[T], E(T)) pair.
+// Warp roles: 0 TMA producer, 1 MMA issuer + TMEM owner, 2-5 epilogue.
+// ===========================================================================
+namespace sdt {
+namespace {
+
+constexpr int MX_THREADS = 192;
+constexpr int MX_BV = 8, MX_BO = 4, MX_NX = 32768;
+constexpr int MX_STAGE = 2 * A_BYTES + 2 * B_BYTES;       // 48 KB
+constexpr int MX_SMEM = MX_NX * 4 + 2 * MX_STAGE + 256;  // + barriers
+constexpr int MX_SMEM_ALLOC = MX_SMEM + 1024;
+
+struct MixedTerm {
+    int8_t r[3], c[3];  // row / column dims of the FP64 definition (see sdt_fused.cu)
+    int8_t sign;
+};
+__constant__ MixedTerm kMxD1[9] = {
+    {{0, 1, 3}, {2, 4, 5}, -1}, {{0, 1, 4}, {2, 3, 5}, +1}, {{0, 1, 5}, {2, 3, 4}, -1},
+    {{1, 2, 3}, {0, 4, 5}, -1}, {{1, 2, 4}, {0, 3, 5}, +1}, {{1, 2, 5}, {0, 3, 4}, -1},
+    {{0, 2, 3}, {1, 4, 5}, +1}, {{0, 2, 4}, {1, 3, 5}, -1}, {{0, 2, 5}, {1, 3, 4}, +1}};
+__constant__ MixedTerm kMxD2[9] = {
+    {{0, 3, 4}, {1, 2, 5}, -1}, {{0, 4, 5}, {1, 2, 3}, -1}, {{0, 3, 5}, {1, 2, 4}, +1},
+    {{1, 3, 4}, {0, 2, 5}, +1}, {{1, 4, 5}, {0, 2, 3}, +1}, {{1, 3, 5}, {0, 2, 4}, -1},
+    {{2, 3, 4}, {0, 1, 5}, -1}, {{2, 4, 5}, {0, 1, 3}, -1}, {{2, 3, 5}, {0, 1, 4}, +1}};
+
+struct MixedParams {
+    CUtensorMap t2b_hi, t2b_lo, t2a_hi, t2a_lo, wd1_hi, wd1_lo;
+    const CUtensorMap *vd2_maps;  // [2*pair]: hi, lo
+    const int32_t *pair_id;       // [nvab*nvab]
+    const double *T1d, *Ud, *evl;
+    const int32_t *tiles;         // [ntiles][4] start, range, spin, sym
+    int32_t noab, nvab, nk_o, nk_v;
+    int64_t nocc, nvir;
+    const int64_t *klist, *item_pref;
+    const double *factor;
+    int64_t n_tasks, item_base;
+    double *part;
+    int *err;
+};
+
+__device__ __forceinline__ int mx_stride(int d) {
+    // master layout [a][b][c][i][j][k], extents 8,8,8,4,4,4
+    return d == 0 ? 4096 : d == 1 ? 512 : d == 2 ? 64 : d == 3 ? 16 : d == 4 ? 4 : 1;
+}
+
+__device__ __forceinline__ void named_bar(int id, int n) {
+    asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(n) : "memory");
+}
+
+__global__ void __launch_bounds__(MX_THREADS, 1) fused_mixed_kernel(const __grid_constant__ MixedParams p) {
+    extern __shared__ __align__(1024) uint8_t smem_raw[];
+    uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    float *X = (float *)smem;
+    uint8_t *stages = smem + MX_NX * 4;
+    uint64_t *bars = (uint64_t *)(stages + 2 * MX_STAGE);
+    uint64_t *full = bars, *empty = bars + 2, *tfull = bars + 4, *tempty = bars + 6, *drain = bars + 8;
+    uint32_t *tslot = (uint32_t *)(bars + 9);
+    volatile int *abort = (volatile int *)(tslot + 1);
+    volatile int *epi_ok = (volatile int *)(tslot + 2);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+
+    // ---- tuple and sub-box of this CTA ----
+    const int64_t item = p.item_base + blockIdx.x;
+    int64_t lo_ = 0, hi_ = p.n_tasks - 1;
+    while (lo_ < hi_) {
+        const int64_t mid = (lo_ + hi_ + 1) >> 1;
+        if (p.item_pref[mid] <= item) lo_ = mid;
+        else hi_ = mid - 1;
+    }
+    const int64_t tq = lo_;
+    int64_t local = item - p.item_pref[tq];
+    int tile[6], ext[6], start[6], boff[6];
+#pragma unroll
+    for (int d = 0; d < 6; ++d) {
+        tile[d] = (int)p.klist[7 * tq + d];
+        start[d] = __ldg(p.tiles + 4 * (tile[d] - 1));
+        ext[d] = __ldg(p.tiles + 4 * (tile[d] - 1) + 1);
+    }
+#pragma unroll
+    for (int d = 5; d >= 0; --d) {
+        const int bx = d < 3 ? MX_BV : MX_BO;
+        const int nb = (ext[d] + bx - 1) / bx;
+        boff[d] = (int)(local % nb) * bx;
+        local /= nb;
+    }
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < 2; ++s) {
+            tc::mbar_init(&full[s], 1);
+            tc::mbar_init(&empty[s], 1);
+            tc::mbar_init(&tfull[s], 1);
+            tc::mbar_init(&tempty[s], 1);
+        }
+        tc::mbar_init(drain, 1);
+        *abort = 0;
+        *epi_ok = 1;
+        tc::fence_mbar_init();
+    }
+    if (warp == 1) tc::tmem_alloc(tslot, 512);
+    for (int e = threadIdx.x; e < MX_NX; e += MX_THREADS) X[e] = 0.0f;
+    tc::tc_fence_before();
+    __syncthreads();
+    tc::tc_fence_after();
+    const uint32_t tmem = *tslot;
+
+    if (warp == 0 && lane == 0) {
+        // ---------------- TMA producer ----------------
+        uint32_t g = 0;
+        bool stop = false;
+        for (int t = 0; t < 18 && !stop; ++t) {
+            const bool d1 = t < 9;
+            const MixedTerm td = d1 ? kMxD1[t] : kMxD2[t - 9];
+            const int nk = d1 ? p.nk_o : p.nk_v;
+            const CUtensorMap *ah, *al, *bh, *bl;
+            int ac1, ac2, ac3, bc1, bc2, bc3;
+            if (d1) {
+                ah = &p.wd1_hi; al = &p.wd1_lo; bh = &p.t2a_hi; bl = &p.t2a_lo;
+                ac1 = start[td.c[2]] + boff[td.c[2]]; ac2 = start[td.c[1]] + boff[td.c[1]];
+                ac3 = start[td.c[0]] + boff[td.c[0]];
+                bc1 = start[td.r[2]] + boff[td.r[2]]; bc2 = start[td.r[1]] + boff[td.r[1]];
+                bc3 = start[td.r[0]] + boff[td.r[0]];
+            } else {
+                ah = &p.t2b_hi; al = &p.t2b_lo;
+                const int pr = p.pair_id[(tile[td.c[0]] - p.noab - 1) * p.nvab + (tile[td.c[1]] - p.noab - 1)];
+                bh = p.vd2_maps + 2 * pr; bl = bh + 1;
+                ac1 = start[td.r[2]] + boff[td.r[2]]; ac2 = start[td.r[1]] + boff[td.r[1]];
+                ac3 = start[td.r[0]] + boff[td.r[0]];
+                bc1 = start[td.c[2]] + boff[td.c[2]]; bc2 = boff[td.c[1]]; bc3 = boff[td.c[0]];
+            }
+            for (int kc = 0; kc < nk; ++kc, ++g) {
+                const int s = g & 1;
+                if (g >= 2 && !tc::mbar_wait(&empty[s], ((g >> 1) & 1) ^ 1, kWaitNs, abort)) {
+                    stop = true;
+                    break;
+                }
+                uint8_t *st = stages + s * MX_STAGE;
+                tc::mbar_arrive_expect_tx(&full[s], MX_STAGE);
+                const int k0 = kc * KC;
+                tc::tma_load_4d(st, ah, &full[s], k0, ac1, ac2, ac3);
+                tc::tma_load_4d(st + A_BYTES, al, &full[s], k0, ac1, ac2, ac3);
+                tc::tma_load_4d(st + 2 * A_BYTES, bh, &full[s], k0, bc1, bc2, bc3);
+                tc::tma_load_4d(st + 2 * A_BYTES + B_BYTES, bl, &full[s], k0, bc1, bc2, bc3);
+            }
+        }
+        if (stop) {
+            *abort = 1;
+            atomicCAS(p.err, 0, 1);
+            // copies already issued must land before the CTA exits
+            volatile int never = 0;
+            for (uint32_t x = g >= 2 ? g - 2 : 0; x < g; ++x)
+                tc::mbar_wait(&full[x & 1], (x >> 1) & 1, kWaitNs, &never);
+        }
+    } else if (warp == 1 && lane == 0) {
+        // ---------------- MMA issuer ----------------
+        const uint32_t idesc = tc::idesc_tf32(128, 256);
+        uint32_t g = 0;
+        bool stop = false;
+        for (int t = 0; t < 18 && !stop; ++t) {
+            const int buf = t & 1;
+            const int nk = t < 9 ? p.nk_o : p.nk_v;
+            if (t >= 2 && !tc::mbar_wait(&tempty[buf], ((t >> 1) - 1) & 1, kWaitNs, abort)) {
+                stop = true;
+                break;
+            }
+            tc::tc_fence_after();
+            const uint32_t d_tmem = tmem + (uint32_t)(buf * 256);
+            for (int kc = 0; kc < nk; ++kc, ++g) {
+                const int s = g & 1;
+                if (!tc::mbar_wait(&full[s], (g >> 1) & 1, kWaitNs, abort)) {
+                    stop = true;
+                    break;
+                }
+                tc::tc_fence_after();
+                const uint32_t st = tc::smem_u32(stages + s * MX_STAGE);
+#pragma unroll
+                for (int kk = 0; kk < KC / 8; ++kk) {
+                    const uint32_t a_h = st + kk * 32, a_l = st + A_BYTES + kk * 32;
+                    const uint32_t b_h = st + 2 * A_BYTES + kk * 32, b_l = st + 2 * A_BYTES + B_BYTES + kk * 32;
+                    tc::mma_tf32(d_tmem, tc::sdesc_sw64(a_h), tc::sdesc_sw64(b_h), idesc,
+                                 (kc == 0 && kk == 0) ? 0u : 1u);
+                    tc::mma_tf32(d_tmem, tc::sdesc_sw64(a_h), tc::sdesc_sw64(b_l), idesc, 1u);
+                    tc::mma_tf32(d_tmem, tc::sdesc_sw64(a_l), tc::sdesc_sw64(b_h), idesc, 1u);
+                }
+                tc::mma_commit(&empty[s]);
+            }
+            if (!stop) tc::mma_commit(&tfull[buf]);
+        }
+        if (stop) {
+            *abort = 1;
+            atomicCAS(p.err, 0, 2);
+        }
+        // every issued MMA completes before TMEM is released
+        tc::mma_commit(drain);
+        volatile int never = 0;
+        tc::mbar_wait(drain, 0, kWaitNs, &never);
+    } else if (warp >= 2) {
+        // ---------------- epilogue: drain TMEM into the sub-box ----------------
+        const int quad = warp & 3;
+        const int m = quad * 32 + lane;  // TMEM lane = GEMM row
+        const bool leader = (warp == 2 && lane == 0);
+        for (int t = 0; t < 18; ++t) {
+            const int buf = t & 1;
+            if (leader) *epi_ok = tc::mbar_wait(&tfull[buf], (t >> 1) & 1, kWaitNs, abort) ? 1 : 0;
+            named_bar(1, 128);
+            if (!*epi_ok) break;
+            tc::tc_fence_after();
+            const bool d1 = t < 9;
+            const MixedTerm td = d1 ? kMxD1[t] : kMxD2[t - 9];
+            // rows: d1 -> (Q,H',H'') = td.c ; d2 -> (P,H,H') = td.r
+            // cols: d1 -> (P,P',H) = td.r ; d2 -> (Q,Q',H'') = td.c
+            const int8_t *rd = d1 ? td.c : td.r;
+            const int8_t *cd = d1 ? td.r : td.c;
+            const int roff = (m >> 4) * mx_stride(rd[0]) + ((m >> 2) & 3) * mx_stride(rd[1]) +
+                             (m & 3) * mx_stride(rd[2]);
+            const int s0 = mx_stride(cd[0]), s1 = mx_stride(cd[1]), s2 = mx_stride(cd[2]);
+            const float sign = (float)td.sign;
+            for (int c = 0; c < 8; ++c) {
+                float v[32];
+                tc::tmem_ld32(tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(buf * 256 + c * 32), v);
+#pragma unroll
+                for (int q = 0; q < 32; ++q) {
+                    const int n = c * 32 + q;
+                    X[roff + (n >> 5) * s0 + ((n >> 2) & 7) * s1 + (n & 3) * s2] += sign * v[q];
+                }
+            }
+            tc::tc_fence_before();
+            named_bar(1, 128);
+            if (leader) tc::mbar_arrive(&tempty[buf]);
+        }
+        if (leader && !*epi_ok) {
+            *abort = 1;
+            atomicCAS(p.err, 0, 3);
+        }
+    }
+    tc::tc_fence_before();
+    __syncthreads();
+    if (warp == 1) {
+        tc::tc_fence_after();
+        tc::tmem_dealloc(tmem, 512);
+    }
+    if (*abort) {
+        if (threadIdx.x == 0) {
+            p.part[2 * item] = 0.0;
+            p.part[2 * item + 1] = 0.0;
+        }
+        return;
+    }
+
+    // ---------------- FP64 epilogue: s1 terms, denominator, energies ----------------
+    const double factor = p.factor[tq];
+    const double *__restrict__ eo = p.evl;
+    const double *__restrict__ ev = p.evl + p.nocc;
+    const int64_t v = p.nvir, o = p.nocc;
+    double e1 = 0.0, e2 = 0.0;
+    for (int e = threadIdx.x; e < MX_NX; e += MX_THREADS) {
+        const int l0 = e >> 12, l1 = (e >> 9) & 7, l2 = (e >> 6) & 7, l3 = (e >> 4) & 3, l4 = (e >> 2) & 3,
+                  l5 = e & 3;
+        if (boff[0] + l0 >= ext[0] || boff[1] + l1 >= ext[1] || boff[2] + l2 >= ext[2] ||
+            boff[3] + l3 >= ext[3] || boff[4] + l4 >= ext[4] || boff[5] + l5 >= ext[5])
+            continue;
+        const int64_t a = start[0] + boff[0] + l0, b = start[1] + boff[1] + l1, c = start[2] + boff[2] + l2;
+        const int64_t i = start[3] + boff[3] + l3, j = start[4] + boff[4] + l4, k = start[5] + boff[5] + l5;
+        auto u = [&](int64_t x, int64_t y, int64_t h, int64_t gg) {
+            return __ldg(p.Ud + ((x * v + y) * o + h) * o + gg);
+        };
+        auto t1 = [&](int64_t x, int64_t h) { return __ldg(p.T1d + x * o + h); };
+        double sing = t1(a, i) * u(b, c, j, k);
+        sing -= t1(a, j) * u(b, c, i, k);
+        sing += t1(a, k) * u(b, c, i, j);
+        sing -= t1(b, i) * u(a, c, j, k);
+        sing += t1(b, j) * u(a, c, i, k);
+        sing -= t1(b, k) * u(a, c, i, j);
+        sing += t1(c, i) * u(a, b, j, k);
+        sing -= t1(c, j) * u(a, b, i, k);
+        sing += t1(c, k) * u(a, b, i, j);
+        const double doub = (double)X[e];
+        const double denom_0 = -(ev[a] + ev[b] + ev[c]);
+        const double denom = doub * factor / (eo[i] + eo[j] + eo[k] + denom_0);
+        e1 += denom * doub;
+        e2 += denom * (doub + sing);
+    }
+    double *red = (double *)stages;  // stages are idle now
+    e1 = warp_sum(e1);
+    e2 = warp_sum(e2);
+    if (lane == 0) {
+        red[2 * warp] = e1;
+        red[2 * warp + 1] = e2;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double x = 0.0, y = 0.0;
+        for (int w = 0; w < MX_THREADS / 32; ++w) {
+            x += red[2 * w];
+            y += red[2 * w + 1];
+        }
+        p.part[2 * item] = x;
+        p.part[2 * item + 1] = y;
+    }
+}
+
+// FP64 rows [rows][n] -> TF32 hi/lo rows [rows][n_pad] (zero padding).
+__global__ void __launch_bounds__(256) split_rows_kernel(const double *__restrict__ src, float *__restrict__ hi,
+                                                         float *__restrict__ lo, int64_t rows, int64_t n,
+                                                         int64_t n_pad) {
+    const int64_t total = rows * n_pad;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t r = i / n_pad, c = i % n_pad;
+        float h = 0.0f, l = 0.0f;
+        if (c < n) {
+            const double x = src[r * n + c];
+            h = tc::to_tf32(__double2float_rn(x));
+            l = tc::to_tf32(__double2float_rn(x - (double)h));
+        }
+        hi[i] = h;
+        lo[i] = l;
+    }
+}
+
+}  // namespace
+
+void mixed_release(sdt_job *j) {
+    for (int k = 0; k < 2 * SP_N; ++k) {
+        gpu_put(j->sp[k]);
+        j->sp[k] = nullptr;
+        j->sp_n[k] = 0;
+    }
+    gpu_put(j->vd2_maps);
+    gpu_put(j->pair_id);
+    gpu_put(j->err_d);
+    host_put(j->err_h);
+    j->vd2_maps = nullptr;
+    j->pair_id = nullptr;
+    j->err_d = nullptr;
+    j->err_h = nullptr;
+    j->mixed_ready = false;
+}
+
+int mixed_prepare(sdt_job *j, cudaStream_t st) {
+    mixed_release(j);
+    const Tiling &t = j->t;
+    const int64_t o = t.nocc, v = t.nvir, noab = t.noab, nvab = t.nvab;
+    const int64_t op = (o + 3) / 4 * 4, vp = (v + 3) / 4 * 4;
+    j->o_pad = op;
+    j->v_pad = vp;
+    struct Src { int idx; int64_t rows, n, npad; };
+    const int64_t vd2_elems = (int64_t)j->arr_n[DST_VD2];
+    const Src src[SP_N] = {{DST_T2A, v * v * o, o, op}, {DST_T2B, v * o * o, v, vp},
+                           {DST_WD1, v * o * o, o, op}, {DST_VD2, vd2_elems / v, v, vp}};
+    for (int k = 0; k < SP_N; ++k) {
+        const size_t n = (size_t)(src[k].rows * src[k].npad);
+        for (int h = 0; h < 2; ++h) {
+            j->sp[2 * k + h] = (float *)gpu_get(std::max<size_t>(n, 1) * sizeof(float));
+            if (!j->sp[2 * k + h]) {
+                mixed_release(j);
+                return fail(SDT_ERR_NOMEM, "mixed form: split operand allocation");
+            }
+            j->sp_n[2 * k + h] = n;
+        }
+        int64_t blocks = std::min<int64_t>((int64_t)(n + 255) / 256, 152 * 16);
+        if (blocks < 1) blocks = 1;
+        split_rows_kernel<<<(unsigned)blocks, 256, 0, st>>>(j->arr[src[k].idx], j->sp[2 * k], j->sp[2 * k + 1],
+                                                            src[k].rows, src[k].n, src[k].npad);
+        count_launch();
+    }
+    int rc = cuda_check(cudaGetLastError(), "mixed form: split");
+    if (rc) return rc;
+    // Tensor maps (fp32, 64-byte swizzle, 16 K elements per box row).
+    const uint64_t B4 = 4;
+    {
+        const uint64_t d[4] = {(uint64_t)vp, (uint64_t)o, (uint64_t)o, (uint64_t)v};
+        const uint64_t sb[3] = {vp * B4, o * vp * B4, o * o * vp * B4};
+        const uint32_t box[4] = {KC, 4, 4, 8};
+        rc = make_tmap_f32(&j->maps[0], j->sp[2 * SP_T2B], 4, d, sb, box);
+        if (!rc) rc = make_tmap_f32(&j->maps[1], j->sp[2 * SP_T2B + 1], 4, d, sb, box);
+    }
+    if (!rc) {
+        const uint64_t d[4] = {(uint64_t)op, (uint64_t)o, (uint64_t)v, (uint64_t)v};
+        const uint64_t sb[3] = {op * B4, o * op * B4, v * o * op * B4};
+        const uint32_t box[4] = {KC, 4, 8, 8};
+        rc = make_tmap_f32(&j->maps[2], j->sp[2 * SP_T2A], 4, d, sb, box);
+        if (!rc) rc = make_tmap_f32(&j->maps[3], j->sp[2 * SP_T2A + 1], 4, d, sb, box);
+    }
+    if (!rc) {
+        const uint64_t d[4] = {(uint64_t)op, (uint64_t)o, (uint64_t)o, (uint64_t)v};
+        const uint64_t sb[3] = {op * B4, o * op * B4, o * o * op * B4};
+        const uint32_t box[4] = {KC, 4, 4, 8};
+        rc = make_tmap_f32(&j->maps[4], j->sp[2 * SP_WD1], 4, d, sb, box);
+        if (!rc) rc = make_tmap_f32(&j->maps[5], j->sp[2 * SP_WD1 + 1], 4, d, sb, box);
+    }
+    std::vector<CUtensorMap> vmaps;
+    std::vector<int32_t> pid(nvab * nvab, -1);
+    for (int64_t B = noab + 1; B <= noab + nvab && !rc; ++B)
+        for (int64_t C = B; C <= noab + nvab && !rc; ++C) {
+            const int64_t off = j->pair_host[(B - noab - 1) * nvab + (C - noab - 1)];
+            const int64_t nB = t.r(B), nC = t.r(C);
+            const int64_t soff = off / v * vp;
+            const uint64_t d[4] = {(uint64_t)vp, (uint64_t)o, (uint64_t)nC, (uint64_t)nB};
+            const uint64_t sb[3] = {vp * B4, o * vp * B4, nC * o * vp * B4};
+            const uint32_t box[4] = {KC, 4, 8, 8};
+            CUtensorMap mh, ml;
+            rc = make_tmap_f32(&mh, j->sp[2 * SP_VD2] + soff, 4, d, sb, box);
+            if (!rc) rc = make_tmap_f32(&ml, j->sp[2 * SP_VD2 + 1] + soff, 4, d, sb, box);
+            pid[(B - noab - 1) * nvab + (C - noab - 1)] = (int32_t)(vmaps.size() / 2);
+            vmaps.push_back(mh);
+            vmaps.push_back(ml);
+        }
+    if (rc) {
+        mixed_release(j);
+        return rc;
+    }
+    j->vd2_maps = (CUtensorMap *)gpu_get(vmaps.size() * sizeof(CUtensorMap));
+    j->pair_id = (int32_t *)gpu_get(pid.size() * sizeof(int32_t));
+    j->err_d = (int *)gpu_get(sizeof(int));
+    j->err_h = (int *)host_get(sizeof(int));
+    if (!j->vd2_maps || !j->pair_id || !j->err_d || !j->err_h) {
+        mixed_release(j);
+        return fail(SDT_ERR_NOMEM, "mixed form: tables");
+    }
+    rc = cuda_check(cudaMemcpyAsync(j->vd2_maps, vmaps.data(), vmaps.size() * sizeof(CUtensorMap),
+                                    cudaMemcpyHostToDevice, st), "mixed form: maps");
+    if (!rc) rc = cuda_check(cudaMemcpyAsync(j->pair_id, pid.data(), pid.size() * sizeof(int32_t),
+                                             cudaMemcpyHostToDevice, st), "mixed form: maps");
+    if (!rc) rc = cuda_check(cudaStreamSynchronize(st), "mixed form: prepare");
+    if (rc) {
+        mixed_release(j);
+        return rc;
+    }
+    j->mixed_ready = true;
+    return SDT_OK;
+}
+
+int mixed_launch(sdt_job *j, int64_t items, int64_t n, cudaStream_t st) {
+    const Tiling &t = j->t;
+    MixedParams p;
+    p.t2b_hi = j->maps[0]; p.t2b_lo = j->maps[1];
+    p.t2a_hi = j->maps[2]; p.t2a_lo = j->maps[3];
+    p.wd1_hi = j->maps[4]; p.wd1_lo = j->maps[5];
+    p.vd2_maps = j->vd2_maps;
+    p.pair_id = j->pair_id;
+    p.T1d = j->arr[DST_T1];
+    p.Ud = j->arr[DST_UD];
+    p.evl = j->evl_d;
+    p.tiles = j->tiles;
+    p.noab = (int32_t)t.noab;
+    p.nvab = (int32_t)t.nvab;
+    p.nocc = t.nocc;
+    p.nvir = t.nvir;
+    p.nk_o = (int32_t)((t.nocc + KC - 1) / KC);
+    p.nk_v = (int32_t)((t.nvir + KC - 1) / KC);
+    p.klist = j->klist_d;
+    p.item_pref = j->pref_d;
+    p.factor = j->factor_d;
+    p.n_tasks = n;
+    p.part = j->part_d;
+    p.err = j->err_d;
+    int rc = cuda_check(cudaFuncSetAttribute(fused_mixed_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             MX_SMEM_ALLOC),
+                        "mixed form: smem attribute");
+    if (!rc) rc = cuda_check(cudaMemsetAsync(j->err_d, 0, sizeof(int), st), "mixed form");
+    if (rc) return rc;
+    const int64_t chunk = 1ll << 30;
+    for (int64_t b0 = 0; b0 < items; b0 += chunk) {
+        p.item_base = b0;
+        const unsigned nb = (unsigned)std::min<int64_t>(chunk, items - b0);
+        fused_mixed_kernel<<<nb, MX_THREADS, MX_SMEM_ALLOC, st>>>(p);
+        count_launch();
+    }
+    rc = cuda_check(cudaGetLastError(), "mixed form: fused kernel");
+    if (!rc) rc = cuda_check(cudaMemcpyAsync(j->err_h, j->err_d, sizeof(int), cudaMemcpyDeviceToHost, st),
+                             "mixed form");
+    return rc;
+}
+
+}  // namespace sdt

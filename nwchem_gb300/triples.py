@@ -22,6 +22,7 @@ from .tiling import Tiling
 
 FILE_T1, FILE_T2, FILE_V2 = 0, 1, 2
 PREC_FP64 = 0
+PREC_MIXED_TF32 = 1
 
 
 @dataclass
