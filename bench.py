@@ -241,6 +241,27 @@ def ours(args) -> None:
 
     kern_avg_s = sum(kern_ms) / len(kern_ms) / 1e3
     achieved = (my_flops / args.steps) / kern_avg_s / 1e12
+
+    # Mixed form (TF32 split products on the tensor cores) on the same steps.
+    job.run(kl[step_ids[0]], stream=stream, precision=ng.PREC_MIXED_TF32)   # builds split operands
+    barrier()
+    ev0.record(stream)
+    mixed_e, mixed_ms = [], []
+    for s in range(args.warmup, args.warmup + args.steps):
+        mixed_e.append(job.run(kl[step_ids[s]], stream=stream, precision=ng.PREC_MIXED_TF32))
+        mixed_ms.append(job.last_kernel_ms)
+    ev1.record(stream)
+    barrier()
+    mixed_t = ev0.elapsed_time(ev1) / 1e3
+    if ws > 1:
+        tt = torch.tensor([mixed_t], dtype=torch.float64, device=dev)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        mixed_t = float(tt[0])
+    mixed_value = total_flops / mixed_t / 1e12
+    mixed_achieved = (my_flops / args.steps) / (sum(mixed_ms) / len(mixed_ms) / 1e3) / 1e12
+    rel_err = [max(abs(m[0] - f[0]) / abs(f[0]), abs(m[1] - f[1]) / abs(f[1])) for m, f in zip(mixed_e, energies)]
+    est_err = [abs((m[1] - m[0]) - (f[1] - f[0])) / abs(f[1] - f[0]) for m, f in zip(mixed_e, energies)]
+    bf16 = _measured_bf16()
     job.close()
 
     if rank == 0:
@@ -271,13 +292,25 @@ def ours(args) -> None:
                     "d2h_bytes_per_step": 16, "steps": e2e_steps},
             "gpu_launches": int(launches),
             "clocks": clocks,
+            "mixed": {
+                "form": "TF32 split products (hi*hi+hi*lo+lo*hi), FP32 accumulation on tcgen05, FP64 epilogue",
+                "value": mixed_value, "unit": "TFLOP/s", "speedup_vs_fp64": mixed_value / value,
+                "max_rel_err_E": max(rel_err), "max_rel_err_EST": max(est_err),
+                "abs_err_E_last_step": abs(mixed_e[-1][1] - energies[-1][1]),
+                "roofline": {"bound": "tensor", "achieved": mixed_achieved, "peak": bf16[0], "unit": "TFLOP/s",
+                             "frac": mixed_achieved / bf16[0], "peak_source": bf16[1],
+                             "split_ceiling": bf16[0] / 6.0,
+                             "note": "algorithmic FLOPs counted once; TF32 runs at half the BF16 rate and each "
+                                     "product is three MMAs, so the split form's ceiling is peak/6"},
+                "kernel": "fused_mixed_kernel",
+            },
         }
         print(json.dumps(line), flush=True)
     if ws > 1:
         dist.destroy_process_group()
 
 
-def profile_case(args) -> None:
+def profile_case(args) -> None:  # noqa: C901
     """Small case for ncu (under 1 GB on the device, operands still larger
     than L2): o=40 as 8/12/20, v=114 as 20,24,30,40, seed 1; the fused
     kernel on `--tuples` tuples from the middle of the weight-ordered list,
@@ -294,12 +327,63 @@ def profile_case(args) -> None:
     with ng.TriplesJob(t) as job:
         job.load(*files)
         job.set_timing(True)
-        job.run(sel)
-        e = job.run(sel)
-        print(json.dumps({"profile_case": True, "tuples": int(len(sel)), "flops": ng.flops(t, sel),
+        prec = ng.PREC_MIXED_TF32 if args.mixed else ng.PREC_FP64
+        job.run(sel, precision=prec)
+        e = job.run(sel, precision=prec)
+        print(json.dumps({"profile_case": True, "mixed": bool(args.mixed), "tuples": int(len(sel)),
+                          "flops": ng.flops(t, sel),
                           "kernel_ms": job.last_kernel_ms, "device_bytes": job.device_bytes,
                           "tflops": ng.flops(t, sel) / job.last_kernel_ms / 1e9, "energies": list(e)}),
               flush=True)
+
+
+def _measured_bf16() -> tuple[float, str]:
+    path = ROOT / "MEASURED_PEAKS.json"
+    try:
+        return float(json.loads(path.read_text())["bf16_tflops"]), "MEASURED_PEAKS.json bf16_tflops (burst)"
+    except (OSError, KeyError, ValueError):
+        return 1900.0, "fallback 1.9 PFLOP/s bf16 (no MEASURED_PEAKS.json)"
+
+
+def workload_o64v512(args) -> None:
+    """o=64 (2x32), v=512 (8x64), seed 2: the mixed form over a strided tenth of
+    the 480-tuple list, and both forms on one tuple for the error."""
+    import torch
+
+    import nwchem_gb300 as ng
+    torch.cuda.set_device(0)
+    t = ng.config_tiling(2)
+    kl = ng.task_list(t)
+    t0 = time.perf_counter()
+    files = ng.synth_inputs(t, 2)
+    gen_s = time.perf_counter() - t0
+    batch = kl[np.arange(0, len(kl), 10)]
+    one = batch[:1]
+    stream = torch.cuda.Stream()
+    with ng.TriplesJob(t) as job:
+        job.load(*files, stream=stream)
+        job.set_timing(True)
+        job.run(one, stream=stream, precision=ng.PREC_MIXED_TF32)
+        m_one = job.run(one, stream=stream, precision=ng.PREC_MIXED_TF32)
+        ms_one = job.last_kernel_ms
+        f_one = job.run(one, stream=stream)
+        fs_one = job.last_kernel_ms
+        mixed = job.run(batch, stream=stream, precision=ng.PREC_MIXED_TF32)
+        ms_batch = job.last_kernel_ms
+        dev_bytes = job.device_bytes
+    fl_one, fl_batch = ng.flops(t, one), ng.flops(t, batch)
+    bf16 = _measured_bf16()
+    ach = fl_batch / (ms_batch / 1e3) / 1e12
+    print(json.dumps({
+        "workload": "o64v512: o=64 as 2x32, v=512 as 8x64, seed 2",
+        "mixed_tuples": int(len(batch)), "mixed_flops": fl_batch, "mixed_kernel_s": ms_batch / 1e3,
+        "mixed_tflops": ach, "mixed_frac_of_bf16_peak": ach / bf16[0], "bf16_peak": bf16[0],
+        "fp64_one_tuple_tflops": fl_one / (fs_one / 1e3) / 1e12,
+        "mixed_one_tuple_tflops": fl_one / (ms_one / 1e3) / 1e12,
+        "one_tuple": [int(x) for x in one[0, :6]],
+        "E_fp64_one_tuple": list(f_one), "E_mixed_one_tuple": list(m_one),
+        "rel_err_E": max(abs(m_one[0] - f_one[0]) / abs(f_one[0]), abs(m_one[1] - f_one[1]) / abs(f_one[1])),
+        "E_mixed_batch": list(mixed), "device_bytes": dev_bytes, "input_generation_s": gen_s}), flush=True)
 
 
 def main() -> None:
@@ -311,12 +395,16 @@ def main() -> None:
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--profile", action="store_true", help="small single-launch case for ncu")
     ap.add_argument("--tuples", type=int, default=2, help="tuples in the --profile case")
+    ap.add_argument("--workload", default="o40v300", choices=["o40v300", "o64v512"])
+    ap.add_argument("--mixed", action="store_true", help="--profile case in the mixed form")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be at least 3")
     import nwchem_gb300.build as b
     b.build()
-    if args.profile:
+    if args.workload == "o64v512":
+        workload_o64v512(args)
+    elif args.profile:
         profile_case(args)
     elif args.impl == "reference":
         reference_arm(args)

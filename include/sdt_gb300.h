@@ -187,6 +187,12 @@ enum { SDT_FILE_T1 = 0, SDT_FILE_T2 = 1, SDT_FILE_V2 = 2 };
 int sdt_synth_file(const sdt_tiling *t, int kind, uint64_t seed,
                    int64_t *nblocks, int64_t *ndata, int64_t *hash,
                    double *data);
+/* Hash table of a TCE file as NWChem lays it out on disk or in a global
+ * array (tce_t1_offset.F, tce_t2_offset.F, tce_mo2e_offset.F): for V2 it
+ * lists every spin/irrep-allowed block, including the kinds the triples
+ * path never reads.  Query sizes with hash == NULL (2*nblocks+1 entries). */
+int sdt_tce_layout(const sdt_tiling *t, int kind, int64_t *nblocks,
+                   int64_t *ndata, int64_t *hash);
 /* Orbital energies: occupied ~ U[-1.5,-0.4], virtual ~ U[0.2,2.5]. */
 int sdt_synth_evl(int64_t nocc, int64_t nvir, uint64_t seed, double *evl);
 

@@ -45,6 +45,7 @@ def _declare(lib):
         "sdt_tasks_flops": (C.c_double, [C.POINTER(SdtTiling), PI64, I64]),
         "sdt_synth_file": (C.c_int, [C.POINTER(SdtTiling), C.c_int, C.c_uint64, PI64, PI64, PI64, PD]),
         "sdt_synth_evl": (C.c_int, [I64, I64, C.c_uint64, PD]),
+        "sdt_tce_layout": (C.c_int, [C.POINTER(SdtTiling), C.c_int, PI64, PI64, PI64]),
         "sdt_job_create": (C.c_int, [C.POINTER(SdtTiling), C.POINTER(C.c_void_p)]),
         "sdt_job_load": (C.c_int, [C.c_void_p, C.POINTER(SdtFile), C.POINTER(SdtFile),
                                    C.POINTER(SdtFile), C.c_void_p]),

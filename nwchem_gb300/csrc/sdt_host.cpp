@@ -285,7 +285,7 @@ struct Block {
     int kind;       // 0 T1, 1 T2, 2 vvov, 3 ovoo, 4 vvoo
 };
 
-std::vector<Block> file_blocks(const Tiling &t, int kind) {
+std::vector<Block> file_blocks(const Tiling &t, int kind, bool full_v2 = false) {
     std::vector<Block> out;
     const int64_t o = t.noab, nt = t.noab + t.nvab, N = nt;
     auto skip_restricted = [&](int64_t ssum, int64_t all_beta) {
@@ -321,6 +321,7 @@ std::vector<Block> file_blocks(const Tiling &t, int kind) {
                         if (v3 && v4 && !v1 && v2) k = 2;        // <p5 p6 || h3 p7>
                         else if (!v3 && v4 && !v1 && !v2) k = 3; // <h7 p6 || h2 h3>
                         else if (v3 && v4 && !v1 && !v2) k = 4;  // <p5 p6 || h2 h3>
+                        else if (full_v2) k = 5;                 // a block the path never reads
                         else continue;
                         if (t.s(g3) + t.s(g4) != t.s(g1) + t.s(g2)) continue;
                         if ((t.y(g3) ^ t.y(g4) ^ t.y(g1) ^ t.y(g2)) != 0) continue;
@@ -388,6 +389,32 @@ extern "C" int sdt_synth_file(const sdt_tiling *ti, int kind, uint64_t seed,
     Gen g(seed, t.nocc, t.nvir);
 #pragma omp parallel for schedule(dynamic, 1)
     for (int64_t q = 0; q < n; ++q) fill_block(t, g, blocks[q], data + offs[q]);
+    return SDT_OK;
+}
+
+// Hash table of a file laid out exactly as NWChem's TCE lays it out
+// (tce_t1_offset.F, tce_t2_offset.F, tce_mo2e_offset.F): blocks in loop
+// order, keys ascending, offsets the running sum of block sizes.  For V2 it
+// covers every (g3b<=g4b, g1b<=g2b) block the spin/irrep rules allow, so an
+// integral file written by NWChem can be read as it is.
+extern "C" int sdt_tce_layout(const sdt_tiling *ti, int kind, int64_t *nblocks, int64_t *ndata,
+                              int64_t *hash) {
+    Tiling t;
+    if (!make_tiling(ti, &t) || kind < 0 || kind > 2 || !nblocks || !ndata)
+        return fail(SDT_ERR_ARG, "sdt_tce_layout: bad argument");
+    std::vector<Block> blocks = file_blocks(t, kind, true);
+    const int64_t n = (int64_t)blocks.size();
+    int64_t total = 0;
+    if (hash) hash[0] = n;
+    for (int64_t q = 0; q < n; ++q) {
+        if (hash) {
+            hash[1 + q] = blocks[q].key;
+            hash[1 + n + q] = total;
+        }
+        total += blocks[q].size;
+    }
+    *nblocks = n;
+    *ndata = total;
     return SDT_OK;
 }
 

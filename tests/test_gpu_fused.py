@@ -147,3 +147,60 @@ def test_box_host_generates_same_inputs(gpu):
     for name, f in zip(("T1", "T2", "V2"), ng.synth_inputs(t, 0)):
         assert hashlib.sha256(f.data.tobytes()).hexdigest() == dig[f"o10v40_seed0_{name}"]["data"]
     assert hashlib.sha256(t.evl.tobytes()).hexdigest() == dig["o10v40_seed0_evl"]
+
+
+def test_fused_reads_nwchem_layout_files(gpu, tmp_path):
+    """T1/T2/V2 in NWChem's on-disk layout (every V2 block; the blocks the path
+    never reads set to NaN) give the FP64 and mixed energies of the synthetic files."""
+    from nwchem_gb300 import tcefile
+    t = ng.Tiling([3, 2, 3], [4, 3, 5]).with_evl(23)
+    files = ng.synth_inputs(t, 23)
+    kinds = (ng.FILE_T1, ng.FILE_T2, ng.FILE_V2)
+    read = []
+    for kind, f in zip(kinds, files):
+        p = tmp_path / f"f{kind}.bin"
+        tcefile.write_tce_file(p, f, t, kind)
+        if kind == ng.FILE_V2:
+            h, nd = tcefile.tce_layout(t, kind)
+            raw = np.fromfile(p, dtype=np.float64)
+            n = int(h[0])
+            for q in range(n):
+                if f.lookup(int(h[1 + q])) < 0:
+                    end = int(h[2 + n + q]) if q + 1 < n else nd
+                    raw[int(h[1 + n + q]):end] = np.nan
+            raw.tofile(p)
+        read.append(tcefile.read_tce_file(p, t, kind, mmap=False))
+    kl = ng.task_list(t)
+    with ng.TriplesJob(t) as a, ng.TriplesJob(t) as b:
+        a.load(*files)
+        b.load(*read)
+        for prec in (ng.PREC_FP64, ng.PREC_MIXED_TF32):
+            assert a.run(kl, precision=prec) == b.run(kl, precision=prec)
+
+
+def test_fused_checkpointed_run(gpu, tmp_path):
+    """A restarted GPU run skips recorded ranges and returns the same bits."""
+    from nwchem_gb300 import restart
+    t = ng.Tiling([3, 5, 2], [4, 6, 4, 3]).with_evl(2)
+    files = ng.synth_inputs(t, 2)
+    kl = ng.task_list(t)
+    with ng.TriplesJob(t) as job:
+        job.load(*files)
+        seen = []
+
+        class Stop(RuntimeError):
+            pass
+
+        def runner(sub):
+            seen.append(len(sub))
+            if len(seen) == 4 and not hasattr(runner, "resumed"):
+                raise Stop()
+            return job.run(sub)
+
+        ck = tmp_path / "c.jsonl"
+        with pytest.raises(Stop):
+            restart.CheckpointedRun(ck, kl, 9, runner).run()
+        runner.resumed = True
+        e = restart.CheckpointedRun(ck, kl, 9, runner).run()
+        full = job.run(kl)
+    assert e[0] == pytest.approx(full[0], rel=1e-13) and e[1] == pytest.approx(full[1], rel=1e-13)
