@@ -219,6 +219,11 @@ int sdt_job_run(sdt_job *job, const int64_t *klist, int64_t n,
 int sdt_job_destroy(sdt_job *job);
 /* Device bytes held by a job. */
 int64_t sdt_job_device_bytes(const sdt_job *job);
+/* Mixed form: drain the tensor-core accumulator every `chunks` K chunks of
+ * 16 (0, the default: once per contraction term).  Shorter accumulation
+ * chains reduce the FP32 rounding of the split products at the cost of more
+ * drains. */
+int sdt_job_set_mixed_segment(sdt_job *job, int chunks);
 /* When on, sdt_job_run brackets its fused-kernel launches with CUDA events
  * on the run's stream; sdt_job_last_kernel_ms returns that interval. */
 int sdt_job_set_timing(sdt_job *job, int on);

@@ -850,3 +850,9 @@ extern "C" int sdt_job_set_timing(sdt_job *j, int on) {
 }
 
 extern "C" double sdt_job_last_kernel_ms(const sdt_job *j) { return j ? (double)j->last_ms : -1.0; }
+
+extern "C" int sdt_job_set_mixed_segment(sdt_job *j, int chunks) {
+    if (!j || chunks < 0) return fail(SDT_ERR_ARG, "sdt_job_set_mixed_segment: bad argument");
+    j->mixed_kseg = chunks;
+    return SDT_OK;
+}

@@ -29,6 +29,7 @@ struct sdt_job {
     size_t sp_n[2 * sdt::SP_N] = {0};
     int64_t o_pad = 0, v_pad = 0;
     bool mixed_ready = false;
+    int mixed_kseg = 0;                  // K chunks per TMEM drain (0: whole term)
     CUtensorMap maps[6];                 // t2b hi/lo, t2a hi/lo, wd1 hi/lo
     CUtensorMap *vd2_maps = nullptr;     // device: 2 per virtual tile pair
     int32_t *pair_id = nullptr;          // device: [nvab*nvab] -> pair index or -1
@@ -58,5 +59,5 @@ int mixed_prepare(sdt_job *j, cudaStream_t st);
 // Launches the mixed fused kernel over the prepared items.
 int mixed_launch(sdt_job *j, int64_t items, int64_t n, cudaStream_t st);
 int make_tmap_f32(CUtensorMap *map, const void *base, int rank, const uint64_t *dims,
-                  const uint64_t *strides_bytes, const uint32_t *box);
+                  const uint64_t *strides_bytes, const uint32_t *box, int swizzle_bytes);
 }  // namespace sdt

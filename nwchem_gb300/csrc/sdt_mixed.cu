@@ -49,7 +49,7 @@ EncodeTiledFn encode_tiled() {
 // fp32 tensor map with 64-byte swizzle; dims innermost first, strides in
 // bytes for dims 1..rank-1.
 int make_tmap_f32(CUtensorMap *map, const void *base, int rank, const uint64_t *dims,
-                  const uint64_t *strides_bytes, const uint32_t *box) {
+                  const uint64_t *strides_bytes, const uint32_t *box, int swizzle_bytes) {
     EncodeTiledFn fn = encode_tiled();
     if (!fn) return fail(SDT_ERR_CUDA, "cuTensorMapEncodeTiled is unavailable");
     if ((reinterpret_cast<uintptr_t>(base) & 15) != 0) return fail(SDT_ERR_ARG, "tensor map base not 16-byte aligned");
@@ -64,9 +64,11 @@ int make_tmap_f32(CUtensorMap *map, const void *base, int rank, const uint64_t *
             gs[i - 1] = strides_bytes[i - 1];
         }
     }
-    if (box[0] * 4 > 64) return fail(SDT_ERR_ARG, "64-byte swizzle needs an inner box of at most 16 fp32");
+    if (swizzle_bytes != 32 && swizzle_bytes != 64) return fail(SDT_ERR_ARG, "swizzle must be 32 or 64 bytes");
+    if ((int)box[0] * 4 > swizzle_bytes) return fail(SDT_ERR_ARG, "tensor map inner box wider than its swizzle");
     CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, rank, const_cast<void *>(base), gd, gs, bx, es,
-                    CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B,
+                    CU_TENSOR_MAP_INTERLEAVE_NONE,
+                    swizzle_bytes == 32 ? CU_TENSOR_MAP_SWIZZLE_32B : CU_TENSOR_MAP_SWIZZLE_64B,
                     CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) return fail(SDT_ERR_CUDA, "cuTensorMapEncodeTiled failed (" + std::to_string((int)r) + ")");
     return SDT_OK;
@@ -205,10 +207,10 @@ extern "C" int sdt_tc_selftest(const float *a_hi, const float *a_lo, const float
     const uint64_t da[2] = {(uint64_t)K, 128}, db[2] = {(uint64_t)K, 256};
     const uint64_t sa[1] = {(uint64_t)K * 4};
     const uint32_t ba[2] = {KC, 128}, bb[2] = {KC, 256};
-    int rc = make_tmap_f32(&g.a_hi, a_hi, 2, da, sa, ba);
-    if (!rc) rc = make_tmap_f32(&g.a_lo, a_lo, 2, da, sa, ba);
-    if (!rc) rc = make_tmap_f32(&g.b_hi, b_hi, 2, db, sa, bb);
-    if (!rc) rc = make_tmap_f32(&g.b_lo, b_lo, 2, db, sa, bb);
+    int rc = make_tmap_f32(&g.a_hi, a_hi, 2, da, sa, ba, 64);
+    if (!rc) rc = make_tmap_f32(&g.a_lo, a_lo, 2, da, sa, ba, 64);
+    if (!rc) rc = make_tmap_f32(&g.b_hi, b_hi, 2, db, sa, bb, 64);
+    if (!rc) rc = make_tmap_f32(&g.b_lo, b_lo, 2, db, sa, bb, 64);
     if (rc) return rc;
     g.K = K;
     g.D = D;
@@ -241,17 +243,25 @@ extern "C" int sdt_tc_selftest(const float *a_hi, const float *a_lo, const float
 //
 // One CTA (192 threads, one per SM) owns an 8x8x8 (a,b,c) x 4x4x4 (i,j,k)
 // sub-box of one tuple's triples tile: 32768 FP32 values in shared memory.
-// Each of the 18 d1/d2 terms is one 128x256xK GEMM on the tensor cores:
-//   d2: A = t(P,e;H,H')  (rows P*16+H*4+H', from T2b), B = v(Q,Q',H'',e)
-//       (cols Q*32+Q'*4+H'', from the Vd2 region of tiles (Q,Q')), K = e;
-//   d1: A = w(m,Q,H',H'') (rows Q*16+H'*4+H'', from Wd1), B = t(P,P';H,m)
-//       (cols P*32+P'*4+H, from T2a), K = m;
-// with operand tiles staged by TMA (64-byte swizzle, 16 K per stage, two
-// stages) and the three split products issued by one thread into one of two
-// TMEM accumulators (256 columns each).  Four epilogue warps drain the other
-// accumulator and add it, with the term's sign, into the sub-box.  The
-// epilogue then promotes to FP64, adds the s1 products and the denominator
-// and writes the CTA's (E[T], E(T)) pair.
+//
+// Each d1 term has exactly the row/column index layout and the sign of one
+// d2 term (d1_1/d2_8, d1_2/d2_9, d1_3/d2_7, d1_4/d2_2, d1_5/d2_3, d1_6/d2_1,
+// d1_7/d2_5, d1_8/d2_6, d1_9/d2_4), so the 18 contractions become 9 merged
+// 128x256 GEMMs with K = o + v into one TMEM accumulator each:
+//   rows (R0;R1,R2) = one particle and two hole indices,
+//   cols (C0,C1;C2) = two particle and one hole index,
+//   D  = sum_m w(m,R0,R1,R2) t(C0,C1;C2,m)     A: Wd1, B: T2a   (K = m)
+//      + sum_e t(R0,e;R1,R2) v(C0,C1,C2,e)     A: T2b, B: Vd2   (K = e)
+// Operand tiles (8 K each) are staged by TMA with 32-byte swizzle in four
+// stages; one thread issues the three split products (hi*hi, hi*lo, lo*hi)
+// into one of two TMEM accumulators of 256 columns.  Four epilogue warps
+// drain the other accumulator into the sub-box with the term's sign.  A term
+// may be drained in K segments of `kseg` chunks, which shortens the tensor
+// cores' FP32 accumulation chains (their rounding error grows with length).
+// The sub-box uses a swizzled hole index so that the 32 rows a warp drains
+// fall in 32 different shared-memory banks for every term layout.  The final
+// epilogue promotes to FP64, adds the s1 products and the denominator and
+// writes the CTA's (E[T], E(T)) pair.
 // Warp roles: 0 TMA producer, 1 MMA issuer + TMEM owner, 2-5 epilogue.
 // ===========================================================================
 namespace sdt {
@@ -259,22 +269,36 @@ namespace {
 
 constexpr int MX_THREADS = 192;
 constexpr int MX_BV = 8, MX_BO = 4, MX_NX = 32768;
-constexpr int MX_STAGE = 2 * A_BYTES + 2 * B_BYTES;       // 48 KB
-constexpr int MX_SMEM = MX_NX * 4 + 2 * MX_STAGE + 256;  // + barriers
+constexpr int MKC = 8;                                    // fp32 K elements per stage (32-byte rows)
+constexpr int MNS = 4;                                    // stages
+constexpr int MA_BYTES = 128 * MKC * 4, MB_BYTES = 256 * MKC * 4;
+constexpr int MX_STAGE = 2 * MA_BYTES + 2 * MB_BYTES;     // 24 KB
+constexpr int MX_SMEM = MX_NX * 4 + MNS * MX_STAGE + 256;
 constexpr int MX_SMEM_ALLOC = MX_SMEM + 1024;
 
-struct MixedTerm {
-    int8_t r[3], c[3];  // row / column dims of the FP64 definition (see sdt_fused.cu)
+// Merged terms: rows (R0;R1,R2), cols (C0,C1;C2), sign.  Dims a=0 b=1 c=2 i=3 j=4 k=5.
+struct MergedTerm {
+    int8_t r[3], c[3];
     int8_t sign;
 };
-__constant__ MixedTerm kMxD1[9] = {
-    {{0, 1, 3}, {2, 4, 5}, -1}, {{0, 1, 4}, {2, 3, 5}, +1}, {{0, 1, 5}, {2, 3, 4}, -1},
-    {{1, 2, 3}, {0, 4, 5}, -1}, {{1, 2, 4}, {0, 3, 5}, +1}, {{1, 2, 5}, {0, 3, 4}, -1},
-    {{0, 2, 3}, {1, 4, 5}, +1}, {{0, 2, 4}, {1, 3, 5}, -1}, {{0, 2, 5}, {1, 3, 4}, +1}};
-__constant__ MixedTerm kMxD2[9] = {
-    {{0, 3, 4}, {1, 2, 5}, -1}, {{0, 4, 5}, {1, 2, 3}, -1}, {{0, 3, 5}, {1, 2, 4}, +1},
-    {{1, 3, 4}, {0, 2, 5}, +1}, {{1, 4, 5}, {0, 2, 3}, +1}, {{1, 3, 5}, {0, 2, 4}, -1},
-    {{2, 3, 4}, {0, 1, 5}, -1}, {{2, 4, 5}, {0, 1, 3}, -1}, {{2, 3, 5}, {0, 1, 4}, +1}};
+__constant__ MergedTerm kMerged[9] = {
+    {{2, 4, 5}, {0, 1, 3}, -1},  // d1_1 + d2_8
+    {{2, 3, 5}, {0, 1, 4}, +1},  // d1_2 + d2_9
+    {{2, 3, 4}, {0, 1, 5}, -1},  // d1_3 + d2_7
+    {{0, 4, 5}, {1, 2, 3}, -1},  // d1_4 + d2_2
+    {{0, 3, 5}, {1, 2, 4}, +1},  // d1_5 + d2_3
+    {{0, 3, 4}, {1, 2, 5}, -1},  // d1_6 + d2_1
+    {{1, 4, 5}, {0, 2, 3}, +1},  // d1_7 + d2_5
+    {{1, 3, 5}, {0, 2, 4}, -1},  // d1_8 + d2_6
+    {{1, 3, 4}, {0, 2, 5}, +1}}; // d1_9 + d2_4
+
+// Sub-box address of local (a,b,c,i,j,k): 64 floats per (a,b,c); inside,
+// bit5 = k>>1, bit4 = (k&1)^parity(a+b+c), bits3-2 = (i+k)&3, bits1-0 = (j+k)&3.
+__device__ __forceinline__ int xaddr(int a, int b, int c, int i, int j, int k) {
+    const int par = (a + b + c) & 1;
+    return ((((a << 3) | b) << 3 | c) << 6) | ((k >> 1) << 5) | ((((k & 1) ^ par)) << 4) |
+           (((i + k) & 3) << 2) | ((j + k) & 3);
+}
 
 struct MixedParams {
     CUtensorMap t2b_hi, t2b_lo, t2a_hi, t2a_lo, wd1_hi, wd1_lo;
@@ -282,7 +306,7 @@ struct MixedParams {
     const int32_t *pair_id;       // [nvab*nvab]
     const double *T1d, *Ud, *evl;
     const int32_t *tiles;         // [ntiles][4] start, range, spin, sym
-    int32_t noab, nvab, nk_o, nk_v;
+    int32_t noab, nvab, nk_o, nk_v, kseg;
     int64_t nocc, nvir;
     const int64_t *klist, *item_pref;
     const double *factor;
@@ -291,13 +315,50 @@ struct MixedParams {
     int *err;
 };
 
-__device__ __forceinline__ int mx_stride(int d) {
-    // master layout [a][b][c][i][j][k], extents 8,8,8,4,4,4
-    return d == 0 ? 4096 : d == 1 ? 512 : d == 2 ? 64 : d == 3 ? 16 : d == 4 ? 4 : 1;
-}
-
 __device__ __forceinline__ void named_bar(int id, int n) {
     asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(n) : "memory");
+}
+
+// Drains 256 columns of TMEM row m for merged term T into the sub-box.
+template <int T>
+__device__ __forceinline__ void drain_term(float *X, uint32_t taddr, int m, float sign) {
+    constexpr int R0 = T < 3 ? 2 : T < 6 ? 0 : 1;
+    constexpr int R1 = (T % 3 == 0) ? 4 : 3;
+    constexpr int R2 = (T % 3 == 2) ? 4 : 5;
+    constexpr int C0 = T < 3 ? 0 : T < 6 ? 1 : 0;
+    constexpr int C1 = T < 3 ? 1 : 2;
+    constexpr int C2 = (T % 3 == 0) ? 3 : (T % 3 == 1) ? 4 : 5;
+    int l[6];
+    l[R0] = m >> 4;
+    l[R1] = (m >> 2) & 3;
+    l[R2] = m & 3;
+#pragma unroll 1
+    for (int cc = 0; cc < 8; ++cc) {
+        float v[32];
+        tc::tmem_ld32(taddr + (uint32_t)(cc * 32), v);
+        l[C0] = cc;
+#pragma unroll
+        for (int q = 0; q < 32; ++q) {
+            l[C1] = q >> 2;
+            l[C2] = q & 3;
+            const int x = xaddr(l[0], l[1], l[2], l[3], l[4], l[5]);
+            X[x] += sign * v[q];
+        }
+    }
+}
+
+__device__ __forceinline__ void drain_any(int t, float *X, uint32_t taddr, int m, float sign) {
+    switch (t) {
+        case 0: drain_term<0>(X, taddr, m, sign); break;
+        case 1: drain_term<1>(X, taddr, m, sign); break;
+        case 2: drain_term<2>(X, taddr, m, sign); break;
+        case 3: drain_term<3>(X, taddr, m, sign); break;
+        case 4: drain_term<4>(X, taddr, m, sign); break;
+        case 5: drain_term<5>(X, taddr, m, sign); break;
+        case 6: drain_term<6>(X, taddr, m, sign); break;
+        case 7: drain_term<7>(X, taddr, m, sign); break;
+        default: drain_term<8>(X, taddr, m, sign); break;
+    }
 }
 
 __global__ void __launch_bounds__(MX_THREADS, 1) fused_mixed_kernel(const __grid_constant__ MixedParams p) {
@@ -305,9 +366,9 @@ __global__ void __launch_bounds__(MX_THREADS, 1) fused_mixed_kernel(const __grid
     uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     float *X = (float *)smem;
     uint8_t *stages = smem + MX_NX * 4;
-    uint64_t *bars = (uint64_t *)(stages + 2 * MX_STAGE);
-    uint64_t *full = bars, *empty = bars + 2, *tfull = bars + 4, *tempty = bars + 6, *drain = bars + 8;
-    uint32_t *tslot = (uint32_t *)(bars + 9);
+    uint64_t *bars = (uint64_t *)(stages + MNS * MX_STAGE);
+    uint64_t *full = bars, *empty = bars + MNS, *tfull = bars + 2 * MNS, *tempty = tfull + 2, *drain = tempty + 2;
+    uint32_t *tslot = (uint32_t *)(drain + 1);
     volatile int *abort = (volatile int *)(tslot + 1);
     volatile int *epi_ok = (volatile int *)(tslot + 2);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -336,11 +397,16 @@ __global__ void __launch_bounds__(MX_THREADS, 1) fused_mixed_kernel(const __grid
         boff[d] = (int)(local % nb) * bx;
         local /= nb;
     }
+    const int nk = p.nk_o + p.nk_v;                    // K chunks of a merged term
+    const int kseg = p.kseg > 0 && p.kseg < nk ? p.kseg : nk;
+    const int nseg = (nk + kseg - 1) / kseg;           // TMEM drains per term
 
     if (threadIdx.x == 0) {
-        for (int s = 0; s < 2; ++s) {
+        for (int s = 0; s < MNS; ++s) {
             tc::mbar_init(&full[s], 1);
             tc::mbar_init(&empty[s], 1);
+        }
+        for (int s = 0; s < 2; ++s) {
             tc::mbar_init(&tfull[s], 1);
             tc::mbar_init(&tempty[s], 1);
         }
@@ -360,39 +426,36 @@ __global__ void __launch_bounds__(MX_THREADS, 1) fused_mixed_kernel(const __grid
         // ---------------- TMA producer ----------------
         uint32_t g = 0;
         bool stop = false;
-        for (int t = 0; t < 18 && !stop; ++t) {
-            const bool d1 = t < 9;
-            const MixedTerm td = d1 ? kMxD1[t] : kMxD2[t - 9];
-            const int nk = d1 ? p.nk_o : p.nk_v;
-            const CUtensorMap *ah, *al, *bh, *bl;
-            int ac1, ac2, ac3, bc1, bc2, bc3;
-            if (d1) {
-                ah = &p.wd1_hi; al = &p.wd1_lo; bh = &p.t2a_hi; bl = &p.t2a_lo;
-                ac1 = start[td.c[2]] + boff[td.c[2]]; ac2 = start[td.c[1]] + boff[td.c[1]];
-                ac3 = start[td.c[0]] + boff[td.c[0]];
-                bc1 = start[td.r[2]] + boff[td.r[2]]; bc2 = start[td.r[1]] + boff[td.r[1]];
-                bc3 = start[td.r[0]] + boff[td.r[0]];
-            } else {
-                ah = &p.t2b_hi; al = &p.t2b_lo;
-                const int pr = p.pair_id[(tile[td.c[0]] - p.noab - 1) * p.nvab + (tile[td.c[1]] - p.noab - 1)];
-                bh = p.vd2_maps + 2 * pr; bl = bh + 1;
-                ac1 = start[td.r[2]] + boff[td.r[2]]; ac2 = start[td.r[1]] + boff[td.r[1]];
-                ac3 = start[td.r[0]] + boff[td.r[0]];
-                bc1 = start[td.c[2]] + boff[td.c[2]]; bc2 = boff[td.c[1]]; bc3 = boff[td.c[0]];
-            }
+        for (int t = 0; t < 9 && !stop; ++t) {
+            const MergedTerm td = kMerged[t];
+            const int gr0 = start[td.r[0]] + boff[td.r[0]], gr1 = start[td.r[1]] + boff[td.r[1]],
+                      gr2 = start[td.r[2]] + boff[td.r[2]];
+            const int gc0 = start[td.c[0]] + boff[td.c[0]], gc1 = start[td.c[1]] + boff[td.c[1]],
+                      gc2 = start[td.c[2]] + boff[td.c[2]];
+            const int pr = p.pair_id[(tile[td.c[0]] - p.noab - 1) * p.nvab + (tile[td.c[1]] - p.noab - 1)];
+            const CUtensorMap *vh = p.vd2_maps + 2 * pr, *vl = vh + 1;
             for (int kc = 0; kc < nk; ++kc, ++g) {
-                const int s = g & 1;
-                if (g >= 2 && !tc::mbar_wait(&empty[s], ((g >> 1) & 1) ^ 1, kWaitNs, abort)) {
+                const int s = g % MNS;
+                if (g >= MNS && !tc::mbar_wait(&empty[s], ((g / MNS) & 1) ^ 1, kWaitNs, abort)) {
                     stop = true;
                     break;
                 }
                 uint8_t *st = stages + s * MX_STAGE;
                 tc::mbar_arrive_expect_tx(&full[s], MX_STAGE);
-                const int k0 = kc * KC;
-                tc::tma_load_4d(st, ah, &full[s], k0, ac1, ac2, ac3);
-                tc::tma_load_4d(st + A_BYTES, al, &full[s], k0, ac1, ac2, ac3);
-                tc::tma_load_4d(st + 2 * A_BYTES, bh, &full[s], k0, bc1, bc2, bc3);
-                tc::tma_load_4d(st + 2 * A_BYTES + B_BYTES, bl, &full[s], k0, bc1, bc2, bc3);
+                if (kc < p.nk_o) {  // d1 part: A = w(m,R0,R1,R2), B = t(C0,C1;C2,m)
+                    const int k0 = kc * MKC;
+                    tc::tma_load_4d(st, &p.wd1_hi, &full[s], k0, gr2, gr1, gr0);
+                    tc::tma_load_4d(st + MA_BYTES, &p.wd1_lo, &full[s], k0, gr2, gr1, gr0);
+                    tc::tma_load_4d(st + 2 * MA_BYTES, &p.t2a_hi, &full[s], k0, gc2, gc1, gc0);
+                    tc::tma_load_4d(st + 2 * MA_BYTES + MB_BYTES, &p.t2a_lo, &full[s], k0, gc2, gc1, gc0);
+                } else {  // d2 part: A = t(R0,e;R1,R2), B = v(C0,C1,C2,e)
+                    const int k0 = (kc - p.nk_o) * MKC;
+                    tc::tma_load_4d(st, &p.t2b_hi, &full[s], k0, gr2, gr1, gr0);
+                    tc::tma_load_4d(st + MA_BYTES, &p.t2b_lo, &full[s], k0, gr2, gr1, gr0);
+                    tc::tma_load_4d(st + 2 * MA_BYTES, vh, &full[s], k0, gc2, boff[td.c[1]], boff[td.c[0]]);
+                    tc::tma_load_4d(st + 2 * MA_BYTES + MB_BYTES, vl, &full[s], k0, gc2, boff[td.c[1]],
+                                    boff[td.c[0]]);
+                }
             }
         }
         if (stop) {
@@ -400,43 +463,42 @@ __global__ void __launch_bounds__(MX_THREADS, 1) fused_mixed_kernel(const __grid
             atomicCAS(p.err, 0, 1);
             // copies already issued must land before the CTA exits
             volatile int never = 0;
-            for (uint32_t x = g >= 2 ? g - 2 : 0; x < g; ++x)
-                tc::mbar_wait(&full[x & 1], (x >> 1) & 1, kWaitNs, &never);
+            for (uint32_t x = g >= MNS ? g - MNS : 0; x < g; ++x)
+                tc::mbar_wait(&full[x % MNS], (x / MNS) & 1, kWaitNs, &never);
         }
     } else if (warp == 1 && lane == 0) {
         // ---------------- MMA issuer ----------------
         const uint32_t idesc = tc::idesc_tf32(128, 256);
-        uint32_t g = 0;
+        uint32_t g = 0, sg = 0;  // chunk and segment counters
         bool stop = false;
-        for (int t = 0; t < 18 && !stop; ++t) {
-            const int buf = t & 1;
-            const int nk = t < 9 ? p.nk_o : p.nk_v;
-            if (t >= 2 && !tc::mbar_wait(&tempty[buf], ((t >> 1) - 1) & 1, kWaitNs, abort)) {
-                stop = true;
-                break;
-            }
-            tc::tc_fence_after();
-            const uint32_t d_tmem = tmem + (uint32_t)(buf * 256);
-            for (int kc = 0; kc < nk; ++kc, ++g) {
-                const int s = g & 1;
-                if (!tc::mbar_wait(&full[s], (g >> 1) & 1, kWaitNs, abort)) {
+        for (int t = 0; t < 9 && !stop; ++t) {
+            for (int sgi = 0; sgi < nseg && !stop; ++sgi, ++sg) {
+                const int buf = sg & 1;
+                if (sg >= 2 && !tc::mbar_wait(&tempty[buf], ((sg >> 1) - 1) & 1, kWaitNs, abort)) {
                     stop = true;
                     break;
                 }
                 tc::tc_fence_after();
-                const uint32_t st = tc::smem_u32(stages + s * MX_STAGE);
-#pragma unroll
-                for (int kk = 0; kk < KC / 8; ++kk) {
-                    const uint32_t a_h = st + kk * 32, a_l = st + A_BYTES + kk * 32;
-                    const uint32_t b_h = st + 2 * A_BYTES + kk * 32, b_l = st + 2 * A_BYTES + B_BYTES + kk * 32;
-                    tc::mma_tf32(d_tmem, tc::sdesc_sw64(a_h), tc::sdesc_sw64(b_h), idesc,
-                                 (kc == 0 && kk == 0) ? 0u : 1u);
-                    tc::mma_tf32(d_tmem, tc::sdesc_sw64(a_h), tc::sdesc_sw64(b_l), idesc, 1u);
-                    tc::mma_tf32(d_tmem, tc::sdesc_sw64(a_l), tc::sdesc_sw64(b_h), idesc, 1u);
+                const uint32_t d_tmem = tmem + (uint32_t)(buf * 256);
+                const int kc_end = min(nk, (sgi + 1) * kseg);
+                for (int kc = sgi * kseg; kc < kc_end; ++kc, ++g) {
+                    const int s = g % MNS;
+                    if (!tc::mbar_wait(&full[s], (g / MNS) & 1, kWaitNs, abort)) {
+                        stop = true;
+                        break;
+                    }
+                    tc::tc_fence_after();
+                    const uint32_t st = tc::smem_u32(stages + s * MX_STAGE);
+                    const uint32_t a_h = st, a_l = st + MA_BYTES;
+                    const uint32_t b_h = st + 2 * MA_BYTES, b_l = st + 2 * MA_BYTES + MB_BYTES;
+                    tc::mma_tf32(d_tmem, tc::sdesc_sw32(a_h), tc::sdesc_sw32(b_h), idesc,
+                                 kc == sgi * kseg ? 0u : 1u);
+                    tc::mma_tf32(d_tmem, tc::sdesc_sw32(a_h), tc::sdesc_sw32(b_l), idesc, 1u);
+                    tc::mma_tf32(d_tmem, tc::sdesc_sw32(a_l), tc::sdesc_sw32(b_h), idesc, 1u);
+                    tc::mma_commit(&empty[s]);
                 }
-                tc::mma_commit(&empty[s]);
+                if (!stop) tc::mma_commit(&tfull[buf]);
             }
-            if (!stop) tc::mma_commit(&tfull[buf]);
         }
         if (stop) {
             *abort = 1;
@@ -451,36 +513,26 @@ __global__ void __launch_bounds__(MX_THREADS, 1) fused_mixed_kernel(const __grid
         const int quad = warp & 3;
         const int m = quad * 32 + lane;  // TMEM lane = GEMM row
         const bool leader = (warp == 2 && lane == 0);
-        for (int t = 0; t < 18; ++t) {
-            const int buf = t & 1;
-            if (leader) *epi_ok = tc::mbar_wait(&tfull[buf], (t >> 1) & 1, kWaitNs, abort) ? 1 : 0;
-            named_bar(1, 128);
-            if (!*epi_ok) break;
-            tc::tc_fence_after();
-            const bool d1 = t < 9;
-            const MixedTerm td = d1 ? kMxD1[t] : kMxD2[t - 9];
-            // rows: d1 -> (Q,H',H'') = td.c ; d2 -> (P,H,H') = td.r
-            // cols: d1 -> (P,P',H) = td.r ; d2 -> (Q,Q',H'') = td.c
-            const int8_t *rd = d1 ? td.c : td.r;
-            const int8_t *cd = d1 ? td.r : td.c;
-            const int roff = (m >> 4) * mx_stride(rd[0]) + ((m >> 2) & 3) * mx_stride(rd[1]) +
-                             (m & 3) * mx_stride(rd[2]);
-            const int s0 = mx_stride(cd[0]), s1 = mx_stride(cd[1]), s2 = mx_stride(cd[2]);
-            const float sign = (float)td.sign;
-            for (int c = 0; c < 8; ++c) {
-                float v[32];
-                tc::tmem_ld32(tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(buf * 256 + c * 32), v);
-#pragma unroll
-                for (int q = 0; q < 32; ++q) {
-                    const int n = c * 32 + q;
-                    X[roff + (n >> 5) * s0 + ((n >> 2) & 7) * s1 + (n & 3) * s2] += sign * v[q];
+        uint32_t sg = 0;
+        bool ok = true;
+        for (int t = 0; t < 9 && ok; ++t) {
+            const float sign = (float)kMerged[t].sign;
+            for (int sgi = 0; sgi < nseg; ++sgi, ++sg) {
+                const int buf = sg & 1;
+                if (leader) *epi_ok = tc::mbar_wait(&tfull[buf], (sg >> 1) & 1, kWaitNs, abort) ? 1 : 0;
+                named_bar(1, 128);
+                if (!*epi_ok) {
+                    ok = false;
+                    break;
                 }
+                tc::tc_fence_after();
+                drain_any(t, X, tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(buf * 256), m, sign);
+                tc::tc_fence_before();
+                named_bar(1, 128);
+                if (leader) tc::mbar_arrive(&tempty[buf]);
             }
-            tc::tc_fence_before();
-            named_bar(1, 128);
-            if (leader) tc::mbar_arrive(&tempty[buf]);
         }
-        if (leader && !*epi_ok) {
+        if (leader && !ok) {
             *abort = 1;
             atomicCAS(p.err, 0, 3);
         }
@@ -526,7 +578,7 @@ __global__ void __launch_bounds__(MX_THREADS, 1) fused_mixed_kernel(const __grid
         sing += t1(c, i) * u(a, b, j, k);
         sing -= t1(c, j) * u(a, b, i, k);
         sing += t1(c, k) * u(a, b, i, j);
-        const double doub = (double)X[e];
+        const double doub = (double)X[xaddr(l0, l1, l2, l3, l4, l5)];
         const double denom_0 = -(ev[a] + ev[b] + ev[c]);
         const double denom = doub * factor / (eo[i] + eo[j] + eo[k] + denom_0);
         e1 += denom * doub;
@@ -623,23 +675,23 @@ int mixed_prepare(sdt_job *j, cudaStream_t st) {
     {
         const uint64_t d[4] = {(uint64_t)vp, (uint64_t)o, (uint64_t)o, (uint64_t)v};
         const uint64_t sb[3] = {vp * B4, o * vp * B4, o * o * vp * B4};
-        const uint32_t box[4] = {KC, 4, 4, 8};
-        rc = make_tmap_f32(&j->maps[0], j->sp[2 * SP_T2B], 4, d, sb, box);
-        if (!rc) rc = make_tmap_f32(&j->maps[1], j->sp[2 * SP_T2B + 1], 4, d, sb, box);
+        const uint32_t box[4] = {MKC, 4, 4, 8};
+        rc = make_tmap_f32(&j->maps[0], j->sp[2 * SP_T2B], 4, d, sb, box, 32);
+        if (!rc) rc = make_tmap_f32(&j->maps[1], j->sp[2 * SP_T2B + 1], 4, d, sb, box, 32);
     }
     if (!rc) {
         const uint64_t d[4] = {(uint64_t)op, (uint64_t)o, (uint64_t)v, (uint64_t)v};
         const uint64_t sb[3] = {op * B4, o * op * B4, v * o * op * B4};
-        const uint32_t box[4] = {KC, 4, 8, 8};
-        rc = make_tmap_f32(&j->maps[2], j->sp[2 * SP_T2A], 4, d, sb, box);
-        if (!rc) rc = make_tmap_f32(&j->maps[3], j->sp[2 * SP_T2A + 1], 4, d, sb, box);
+        const uint32_t box[4] = {MKC, 4, 8, 8};
+        rc = make_tmap_f32(&j->maps[2], j->sp[2 * SP_T2A], 4, d, sb, box, 32);
+        if (!rc) rc = make_tmap_f32(&j->maps[3], j->sp[2 * SP_T2A + 1], 4, d, sb, box, 32);
     }
     if (!rc) {
         const uint64_t d[4] = {(uint64_t)op, (uint64_t)o, (uint64_t)o, (uint64_t)v};
         const uint64_t sb[3] = {op * B4, o * op * B4, o * o * op * B4};
-        const uint32_t box[4] = {KC, 4, 4, 8};
-        rc = make_tmap_f32(&j->maps[4], j->sp[2 * SP_WD1], 4, d, sb, box);
-        if (!rc) rc = make_tmap_f32(&j->maps[5], j->sp[2 * SP_WD1 + 1], 4, d, sb, box);
+        const uint32_t box[4] = {MKC, 4, 4, 8};
+        rc = make_tmap_f32(&j->maps[4], j->sp[2 * SP_WD1], 4, d, sb, box, 32);
+        if (!rc) rc = make_tmap_f32(&j->maps[5], j->sp[2 * SP_WD1 + 1], 4, d, sb, box, 32);
     }
     std::vector<CUtensorMap> vmaps;
     std::vector<int32_t> pid(nvab * nvab, -1);
@@ -650,10 +702,10 @@ int mixed_prepare(sdt_job *j, cudaStream_t st) {
             const int64_t soff = off / v * vp;
             const uint64_t d[4] = {(uint64_t)vp, (uint64_t)o, (uint64_t)nC, (uint64_t)nB};
             const uint64_t sb[3] = {vp * B4, o * vp * B4, nC * o * vp * B4};
-            const uint32_t box[4] = {KC, 4, 8, 8};
+            const uint32_t box[4] = {MKC, 4, 8, 8};
             CUtensorMap mh, ml;
-            rc = make_tmap_f32(&mh, j->sp[2 * SP_VD2] + soff, 4, d, sb, box);
-            if (!rc) rc = make_tmap_f32(&ml, j->sp[2 * SP_VD2 + 1] + soff, 4, d, sb, box);
+            rc = make_tmap_f32(&mh, j->sp[2 * SP_VD2] + soff, 4, d, sb, box, 32);
+            if (!rc) rc = make_tmap_f32(&ml, j->sp[2 * SP_VD2 + 1] + soff, 4, d, sb, box, 32);
             pid[(B - noab - 1) * nvab + (C - noab - 1)] = (int32_t)(vmaps.size() / 2);
             vmaps.push_back(mh);
             vmaps.push_back(ml);
@@ -699,8 +751,9 @@ int mixed_launch(sdt_job *j, int64_t items, int64_t n, cudaStream_t st) {
     p.nvab = (int32_t)t.nvab;
     p.nocc = t.nocc;
     p.nvir = t.nvir;
-    p.nk_o = (int32_t)((t.nocc + KC - 1) / KC);
-    p.nk_v = (int32_t)((t.nvir + KC - 1) / KC);
+    p.nk_o = (int32_t)((t.nocc + MKC - 1) / MKC);
+    p.nk_v = (int32_t)((t.nvir + MKC - 1) / MKC);
+    p.kseg = j->mixed_kseg;
     p.klist = j->klist_d;
     p.item_pref = j->pref_d;
     p.factor = j->factor_d;

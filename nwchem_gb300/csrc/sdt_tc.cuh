@@ -112,6 +112,18 @@ __device__ __forceinline__ uint64_t sdesc_sw64(uint32_t saddr) {
     return d;
 }
 
+// The same for a K-major tile with 32-byte swizzle: 32-byte rows (8 fp32),
+// 8-row groups 256 bytes apart, layout 6 = 32-byte swizzle.
+__device__ __forceinline__ uint64_t sdesc_sw32(uint32_t saddr) {
+    uint64_t d = 0;
+    d |= (uint64_t)((saddr >> 4) & 0x3FFF);
+    d |= (uint64_t)1 << 16;
+    d |= (uint64_t)(256 >> 4) << 32;
+    d |= (uint64_t)1 << 46;
+    d |= (uint64_t)6 << 61;
+    return d;
+}
+
 // Instruction descriptor, kind::tf32: D = F32 (bits 4-5 = 1), A and B TF32
 // (bits 7-9 and 10-12 = 2), both K-major, N >> 3 at bit 17, M >> 4 at bit 24.
 __host__ __device__ constexpr uint32_t idesc_tf32(int M, int N) {

@@ -128,6 +128,11 @@ class TriplesJob:
         """Bracket the fused launches of each run with CUDA events."""
         _capi.check(self._lib.sdt_job_set_timing(self._h, 1 if on else 0), "sdt_job_set_timing")
 
+    def set_mixed_segment(self, chunks: int) -> None:
+        """Mixed form: drain the tensor-core accumulator every `chunks` K chunks
+        of 16 (0: once per contraction term)."""
+        _capi.check(self._lib.sdt_job_set_mixed_segment(self._h, int(chunks)), "sdt_job_set_mixed_segment")
+
     @property
     def last_kernel_ms(self) -> float:
         return float(self._lib.sdt_job_last_kernel_ms(self._h))

@@ -78,3 +78,19 @@ def test_mixed_matches_fp64_and_oracle(cuda_device, occ, vir, osym, vsym):
     assert m1 == pytest.approx(e1, rel=2e-6) and m2 == pytest.approx(e2, rel=2e-6)
     assert np.abs(mpt - pt).max() <= 2e-6 * max(abs(e1), abs(e2))
     assert (m1b, m2b) == (m1, m2)          # deterministic
+
+
+@pytest.mark.parametrize("kseg", [0, 1, 3])
+def test_mixed_segmented_drains(cuda_device, kseg):
+    """Draining the accumulator in K segments gives the same energies (to the
+    mixed form's bound) as one drain per term."""
+    import nwchem_gb300 as ng
+    t = ng.Tiling([3, 5, 2], [9, 6, 10, 3]).with_evl(5)
+    files = ng.synth_inputs(t, 5)
+    kl = ng.task_list(t)
+    with ng.TriplesJob(t) as job:
+        job.load(*files)
+        f = job.run(kl)
+        job.set_mixed_segment(kseg)
+        m = job.run(kl, precision=ng.PREC_MIXED_TF32)
+    assert m[0] == pytest.approx(f[0], rel=2e-6) and m[1] == pytest.approx(f[1], rel=2e-6)
