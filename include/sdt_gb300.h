@@ -198,11 +198,14 @@ int sdt_synth_evl(int64_t nocc, int64_t nvir, uint64_t seed, double *evl);
 
 /* A job holds one (T) problem resident on the device. */
 typedef struct sdt_job sdt_job;
-/* Precision of sdt_job_run: FP64 throughout, or the mixed form (d1/d2
- * contractions as TF32 split products hi*hi + hi*lo + lo*hi with FP32
- * accumulation on the tensor cores; triples promoted to FP64 before the
- * s1 terms, the denominator and the energy sums). */
-enum { SDT_PREC_FP64 = 0, SDT_PREC_MIXED_TF32 = 1 };
+/* Precision of sdt_job_run: FP64 throughout, or a mixed form: the d1/d2
+ * contractions as split products hi*hi + hi*lo + lo*hi with FP32
+ * accumulation on the tensor cores (TF32x3; BF16x3; FP16x3 with
+ * power-of-two operand scaling), the s1 products in FP32, and the
+ * triples promoted to FP64 for the denominator, the division and the
+ * energy sums. */
+enum { SDT_PREC_FP64 = 0, SDT_PREC_MIXED_TF32 = 1, SDT_PREC_MIXED_BF16 = 2,
+       SDT_PREC_MIXED_FP16 = 3 };
 int sdt_job_create(const sdt_tiling *t, sdt_job **job);
 /* Copy the host TCE files to the device and re-lay them out for the fused
  * kernel (antisymmetric mirrors, signs of tce_hashnsort.F).  Device-side
@@ -219,8 +222,9 @@ int sdt_job_run(sdt_job *job, const int64_t *klist, int64_t n,
 int sdt_job_destroy(sdt_job *job);
 /* Device bytes held by a job. */
 int64_t sdt_job_device_bytes(const sdt_job *job);
-/* Mixed form: drain the tensor-core accumulator every `chunks` K chunks of
- * 16 (0, the default: once per contraction term).  Shorter accumulation
+/* Mixed form: drain the tensor-core accumulator every `chunks` K chunks
+ * (8 TF32 or 16 BF16/FP16 values each; 0, the default: once per
+ * contraction term).  Shorter accumulation
  * chains reduce the FP32 rounding of the split products at the cost of more
  * drains. */
 int sdt_job_set_mixed_segment(sdt_job *job, int chunks);
@@ -253,6 +257,14 @@ double sdt_probe_fp64_tflops(int ms);
  * SDT_ERR_TIMEOUT if a bounded wait in the kernel ran out. */
 int sdt_tc_selftest(const float *a_hi, const float *a_lo, const float *b_hi,
                     const float *b_lo, int K, float *D);
+/* The same with 16-bit operands (bf16 != 0: BF16, else FP16; raw 16-bit
+ * values in device arrays, K a multiple of 8), kind::f16 MMAs. */
+int sdt_tc_selftest16(const void *a_hi, const void *a_lo, const void *b_hi,
+                      const void *b_lo, int K, int bf16, float *D);
+/* Check of the FP64 division of the mixed form's energy epilogue (no
+ * reference counterpart): largest relative difference from the IEEE
+ * quotient over n seeded (numerator, denominator) pairs. */
+int sdt_check_division(int64_t n, uint64_t seed, double *max_rel_err);
 
 #ifdef __cplusplus
 }

@@ -60,6 +60,9 @@ def _declare(lib):
         "sdt_job_last_kernel_ms": (C.c_double, [C.c_void_p]),
         "sdt_probe_fp64_tflops": (C.c_double, [C.c_int]),
         "sdt_tc_selftest": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]),
+        "sdt_tc_selftest16": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int,
+                                        C.c_void_p]),
+        "sdt_check_division": (C.c_int, [C.c_int64, C.c_uint64, C.POINTER(C.c_double)]),
         "compute_en_": (None, [PD, PD, PD, PD, PD, PD, PD, PD, PI64, PI64, PI64, PI64, PI64, PI64, PD, PD]),
         "dev_mem_d_": (None, [PI64] * 6),
         "dev_mem_s_": (None, [PI64] * 6),

@@ -680,9 +680,10 @@ extern "C" int sdt_job_run(sdt_job *j, const int64_t *klist, int64_t n, int prec
                            double *energy, double *per_task, void *stream) {
     if (!j || !energy || (n > 0 && !klist)) return fail(SDT_ERR_ARG, "sdt_job_run: null argument");
     if (!j->loaded) return fail(SDT_ERR_STATE, "sdt_job_run: sdt_job_load has not succeeded");
-    if (precision != SDT_PREC_FP64 && precision != SDT_PREC_MIXED_TF32)
+    if (precision < SDT_PREC_FP64 || precision > SDT_PREC_MIXED_FP16)
         return fail(SDT_ERR_ARG, "sdt_job_run: unknown precision");
-    const bool mixed = precision == SDT_PREC_MIXED_TF32;
+    const bool mixed = precision != SDT_PREC_FP64;
+    const int mtype = precision == SDT_PREC_MIXED_TF32 ? TM_F32 : precision == SDT_PREC_MIXED_BF16 ? TM_BF16 : TM_F16;
     // Sub-box edges: 4 in every index (FP64); 8 virtual x 4 occupied (mixed).
     const int box_v = mixed ? 8 : BOX, box_o = BOX;
     energy[0] = energy[1] = 0.0;
@@ -743,8 +744,8 @@ extern "C" int sdt_job_run(sdt_job *j, const int64_t *klist, int64_t n, int prec
     if (rc) return rc;
 
     if (mixed) {
-        if (!j->mixed_ready) {
-            rc = mixed_prepare(j, st);
+        if (j->mixed_type != mtype) {
+            rc = mixed_prepare(j, mtype, st);
             if (rc) return rc;
         }
         if (j->timing) {

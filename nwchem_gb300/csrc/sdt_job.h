@@ -7,8 +7,10 @@
 
 namespace sdt {
 enum { DST_T1 = 0, DST_T2A, DST_T2B, DST_VD2, DST_WD1, DST_UD, DST_N };
-// TF32 hi/lo copies of the contraction operands (mixed form).
+// Split (hi/lo) copies of the contraction operands (mixed form).
 enum { SP_T2A = 0, SP_T2B, SP_WD1, SP_VD2, SP_N };
+// Operand element types of the mixed form (tensor maps, split copies).
+enum { TM_F32 = 0, TM_BF16 = 1, TM_F16 = 2 };
 }  // namespace sdt
 
 struct sdt_job {
@@ -24,11 +26,15 @@ struct sdt_job {
     double *arr[sdt::DST_N] = {nullptr};
     size_t arr_n[sdt::DST_N] = {0};
     std::vector<int64_t> pair_host;     // Vd2 region offsets (fp64 elements), -1 if none
-    // mixed form: split operands (hi at [2*k], lo at [2*k+1]) and tensor maps
-    float *sp[2 * sdt::SP_N] = {nullptr};
-    size_t sp_n[2 * sdt::SP_N] = {0};
+    // mixed form: split operands (hi at [2*k], lo at [2*k+1]; fp32 holding
+    // TF32 values, or bf16 / fp16), FP32 copies of T1d and Ud for the s1
+    // terms, and tensor maps
+    void *sp[2 * sdt::SP_N] = {nullptr};
+    size_t sp_n[2 * sdt::SP_N] = {0};    // elements
+    int mixed_type = -1;                 // TM_* of the prepared copies, -1: none
+    float *t1f = nullptr, *uf = nullptr;
+    double inv_s = 1.0, inv_s2 = 1.0;    // FP16: 1/(s_T s_I), its square
     int64_t o_pad = 0, v_pad = 0;
-    bool mixed_ready = false;
     int mixed_kseg = 0;                  // K chunks per TMEM drain (0: whole term)
     CUtensorMap maps[6];                 // t2b hi/lo, t2a hi/lo, wd1 hi/lo
     CUtensorMap *vd2_maps = nullptr;     // device: 2 per virtual tile pair
@@ -54,10 +60,11 @@ namespace sdt {
 int finish_run(sdt_job *j, int64_t n, cudaStream_t st);
 // Frees the mixed-form operands and maps of a job.
 void mixed_release(sdt_job *j);
-// Builds the split operands and tensor maps (after a successful load).
-int mixed_prepare(sdt_job *j, cudaStream_t st);
-// Launches the mixed fused kernel over the prepared items.
+// Builds the split operands of element type `type` (TM_*) and the tensor
+// maps (after a successful load).
+int mixed_prepare(sdt_job *j, int type, cudaStream_t st);
+// Launches the persistent mixed kernel over the prepared items.
 int mixed_launch(sdt_job *j, int64_t items, int64_t n, cudaStream_t st);
-int make_tmap_f32(CUtensorMap *map, const void *base, int rank, const uint64_t *dims,
-                  const uint64_t *strides_bytes, const uint32_t *box, int swizzle_bytes);
+int make_tmap(CUtensorMap *map, const void *base, int type, int rank, const uint64_t *dims,
+              const uint64_t *strides_bytes, const uint32_t *box, int swizzle_bytes);
 }  // namespace sdt

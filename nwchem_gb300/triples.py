@@ -22,7 +22,10 @@ from .tiling import Tiling
 
 FILE_T1, FILE_T2, FILE_V2 = 0, 1, 2
 PREC_FP64 = 0
-PREC_MIXED_TF32 = 1
+PREC_MIXED_TF32 = 1   # TF32x3: hi*hi + hi*lo + lo*hi of TF32 pairs
+PREC_MIXED_BF16 = 2   # BF16x3
+PREC_MIXED_FP16 = 3   # FP16x3 with power-of-two operand scaling
+PREC_MIXED = (PREC_MIXED_TF32, PREC_MIXED_BF16, PREC_MIXED_FP16)
 
 
 @dataclass
@@ -130,7 +133,7 @@ class TriplesJob:
 
     def set_mixed_segment(self, chunks: int) -> None:
         """Mixed form: drain the tensor-core accumulator every `chunks` K chunks
-        of 16 (0: once per contraction term)."""
+        (8 TF32 or 16 BF16/FP16 values each; 0: once per contraction term)."""
         _capi.check(self._lib.sdt_job_set_mixed_segment(self._h, int(chunks)), "sdt_job_set_mixed_segment")
 
     @property
