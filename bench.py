@@ -40,6 +40,10 @@ SEED = 1
 WORKLOAD = ("o40v300 tiled FP64 drop-in: o=40 as 8/12/20, v=300 as 20,24x5,30x4,40, seed 1; "
             "step = one of 128 strided slices of the 2860-tuple weight-ordered list")
 METRIC = "(T) TFLOP/s"
+MIXED_FORMS = (("tf32", 1), ("bf16", 2), ("fp16", 3))
+MIXED_NOTE = {"tf32": "TF32x3: TF32 hi/lo pairs, kind::tf32", "bf16": "BF16x3: bf16 hi/lo pairs, kind::f16",
+              "fp16": "FP16x3: fp16 hi/lo pairs of power-of-two scaled operands, kind::f16",
+              "all": "FP32 accumulation in TMEM; s1 products FP32; denominator, division and energy sums FP64"}
 
 
 def _slices(n_tasks: int) -> list[np.ndarray]:
@@ -242,26 +246,37 @@ def ours(args) -> None:
     kern_avg_s = sum(kern_ms) / len(kern_ms) / 1e3
     achieved = (my_flops / args.steps) / kern_avg_s / 1e12
 
-    # Mixed form (TF32 split products on the tensor cores) on the same steps.
-    job.run(kl[step_ids[0]], stream=stream, precision=ng.PREC_MIXED_TF32)   # builds split operands
-    barrier()
-    ev0.record(stream)
-    mixed_e, mixed_ms = [], []
-    for s in range(args.warmup, args.warmup + args.steps):
-        mixed_e.append(job.run(kl[step_ids[s]], stream=stream, precision=ng.PREC_MIXED_TF32))
-        mixed_ms.append(job.last_kernel_ms)
-    ev1.record(stream)
-    barrier()
-    mixed_t = ev0.elapsed_time(ev1) / 1e3
-    if ws > 1:
-        tt = torch.tensor([mixed_t], dtype=torch.float64, device=dev)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        mixed_t = float(tt[0])
-    mixed_value = total_flops / mixed_t / 1e12
-    mixed_achieved = (my_flops / args.steps) / (sum(mixed_ms) / len(mixed_ms) / 1e3) / 1e12
-    rel_err = [max(abs(m[0] - f[0]) / abs(f[0]), abs(m[1] - f[1]) / abs(f[1])) for m, f in zip(mixed_e, energies)]
-    est_err = [abs((m[1] - m[0]) - (f[1] - f[0])) / abs(f[1] - f[0]) for m, f in zip(mixed_e, energies)]
+    # Mixed forms (split products on the tensor cores) on the same steps.
     bf16 = _measured_bf16()
+    mixed = {}
+    for form, prec in MIXED_FORMS:
+        job.run(kl[step_ids[0]], stream=stream, precision=prec)   # builds the split operands
+        barrier()
+        ev0.record(stream)
+        mixed_e, mixed_ms = [], []
+        for s in range(args.warmup, args.warmup + args.steps):
+            mixed_e.append(job.run(kl[step_ids[s]], stream=stream, precision=prec))
+            mixed_ms.append(job.last_kernel_ms)
+        ev1.record(stream)
+        barrier()
+        mixed_t = ev0.elapsed_time(ev1) / 1e3
+        if ws > 1:
+            tt = torch.tensor([mixed_t], dtype=torch.float64, device=dev)
+            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+            mixed_t = float(tt[0])
+        mv = total_flops / mixed_t / 1e12
+        ach = (my_flops / args.steps) / (sum(mixed_ms) / len(mixed_ms) / 1e3) / 1e12
+        rel = [max(abs(m[0] - f[0]) / abs(f[0]), abs(m[1] - f[1]) / abs(f[1])) for m, f in zip(mixed_e, energies)]
+        est = [abs((m[1] - m[0]) - (f[1] - f[0])) / abs(f[1] - f[0]) for m, f in zip(mixed_e, energies)]
+        ceiling = bf16[0] / (6.0 if form == "tf32" else 3.0)
+        mixed[form] = {
+            "value": mv, "unit": "TFLOP/s", "speedup_vs_fp64": mv / value,
+            "max_rel_err_E": max(rel), "max_rel_err_EST": max(est),
+            "abs_err_E_last_step": abs(mixed_e[-1][1] - energies[-1][1]),
+            "roofline": {"bound": "tensor", "achieved": ach, "peak": bf16[0], "unit": "TFLOP/s",
+                         "frac": ach / bf16[0], "peak_source": bf16[1], "split_ceiling": ceiling,
+                         "frac_of_split_ceiling": ach / ceiling},
+        }
     job.close()
 
     if rank == 0:
@@ -293,17 +308,10 @@ def ours(args) -> None:
             "gpu_launches": int(launches),
             "clocks": clocks,
             "mixed": {
-                "form": "TF32 split products (hi*hi+hi*lo+lo*hi), FP32 accumulation on tcgen05, FP64 epilogue",
-                "value": mixed_value, "unit": "TFLOP/s", "speedup_vs_fp64": mixed_value / value,
-                "max_rel_err_E": max(rel_err), "max_rel_err_EST": max(est_err),
-                "abs_err_E_last_step": abs(mixed_e[-1][1] - energies[-1][1]),
-                "roofline": {"bound": "tensor", "achieved": mixed_achieved, "peak": bf16[0], "unit": "TFLOP/s",
-                             "frac": mixed_achieved / bf16[0], "peak_source": bf16[1],
-                             "split_ceiling": bf16[0] / 6.0,
-                             "note": "algorithmic FLOPs counted once; TF32 runs at half the BF16 rate and each "
-                                     "product is three MMAs, so the split form's ceiling is peak/6"},
-                "kernel": "fused_mixed_kernel",
-            },
+                "forms": MIXED_NOTE, "kernel": "split_fused_kernel", **mixed,
+                "note": "algorithmic FLOPs counted once; each product is three MMAs (hi*hi+hi*lo+lo*hi) and "
+                        "TF32 runs at half the BF16 rate, so the split ceilings are peak/3 (BF16, FP16) "
+                        "and peak/6 (TF32)"},
         }
         print(json.dumps(line), flush=True)
     if ws > 1:
@@ -311,26 +319,34 @@ def ours(args) -> None:
 
 
 def profile_case(args) -> None:  # noqa: C901
-    """Small case for ncu (under 1 GB on the device, operands still larger
-    than L2): o=40 as 8/12/20, v=114 as 20,24,30,40, seed 1; the fused
-    kernel on `--tuples` tuples from the middle of the weight-ordered list,
-    one warm-up launch then one launch."""
+    """Small case for ncu, one warm-up launch then one launch of the fused
+    kernel on `--tuples` tuples: --case o40v114 (under 1 GB on the device,
+    operands still larger than L2): o=40 as 8/12/20, v=114 as 20,24,30,40,
+    seed 1, tuples from the middle of the weight-ordered list; --case o64v128
+    (about 4 GB): o=64 as 2x32, v=128 as 2x64, seed 2, the first tuples."""
     import torch
 
     import nwchem_gb300 as ng
     torch.cuda.set_device(0)
-    t = ng.Tiling([8, 12, 20], [20, 24, 30, 40], name="o40v114").with_evl(SEED)
-    kl = ng.task_list(t)
-    files = ng.synth_inputs(t, SEED)
-    mid = len(kl) // 2
-    sel = kl[mid:mid + args.tuples]
+    if args.case == "o64v128":
+        # whole 8x8x8x4x4x4 sub-boxes, as in the o=64/v=512 workload
+        t = ng.Tiling([32, 32], [64, 64], name="o64v128").with_evl(2)
+        files = ng.synth_inputs(t, 2)
+        kl = ng.task_list(t)
+        sel = kl[:args.tuples]
+    else:
+        t = ng.Tiling([8, 12, 20], [20, 24, 30, 40], name="o40v114").with_evl(SEED)
+        kl = ng.task_list(t)
+        files = ng.synth_inputs(t, SEED)
+        mid = len(kl) // 2
+        sel = kl[mid:mid + args.tuples]
     with ng.TriplesJob(t) as job:
         job.load(*files)
         job.set_timing(True)
-        prec = ng.PREC_MIXED_TF32 if args.mixed else ng.PREC_FP64
+        prec = dict(MIXED_FORMS).get(args.mixed, ng.PREC_FP64)
         job.run(sel, precision=prec)
         e = job.run(sel, precision=prec)
-        print(json.dumps({"profile_case": True, "mixed": bool(args.mixed), "tuples": int(len(sel)),
+        print(json.dumps({"profile_case": args.case, "form": args.mixed or "fp64", "tuples": int(len(sel)),
                           "flops": ng.flops(t, sel),
                           "kernel_ms": job.last_kernel_ms, "device_bytes": job.device_bytes,
                           "tflops": ng.flops(t, sel) / job.last_kernel_ms / 1e9, "energies": list(e)}),
@@ -346,8 +362,8 @@ def _measured_bf16() -> tuple[float, str]:
 
 
 def workload_o64v512(args) -> None:
-    """o=64 (2x32), v=512 (8x64), seed 2: the mixed form over a strided tenth of
-    the 480-tuple list, and both forms on one tuple for the error."""
+    """o=64 (2x32), v=512 (8x64), seed 2: each mixed form over a strided tenth
+    of the 480-tuple list, and every form plus FP64 on one tuple for the error."""
     import torch
 
     import nwchem_gb300 as ng
@@ -359,31 +375,33 @@ def workload_o64v512(args) -> None:
     gen_s = time.perf_counter() - t0
     batch = kl[np.arange(0, len(kl), 10)]
     one = batch[:1]
+    fl_one, fl_batch = ng.flops(t, one), ng.flops(t, batch)
+    bf16 = _measured_bf16()
     stream = torch.cuda.Stream()
+    out = {"workload": "o64v512: o=64 as 2x32, v=512 as 8x64, seed 2", "one_tuple": [int(x) for x in one[0, :6]],
+           "batch_tuples": int(len(batch)), "batch_flops": fl_batch, "bf16_peak": bf16[0], "kseg": args.kseg,
+           "input_generation_s": gen_s}
     with ng.TriplesJob(t) as job:
         job.load(*files, stream=stream)
         job.set_timing(True)
-        job.run(one, stream=stream, precision=ng.PREC_MIXED_TF32)
-        m_one = job.run(one, stream=stream, precision=ng.PREC_MIXED_TF32)
-        ms_one = job.last_kernel_ms
+        job.set_mixed_segment(args.kseg)
         f_one = job.run(one, stream=stream)
-        fs_one = job.last_kernel_ms
-        mixed = job.run(batch, stream=stream, precision=ng.PREC_MIXED_TF32)
-        ms_batch = job.last_kernel_ms
-        dev_bytes = job.device_bytes
-    fl_one, fl_batch = ng.flops(t, one), ng.flops(t, batch)
-    bf16 = _measured_bf16()
-    ach = fl_batch / (ms_batch / 1e3) / 1e12
-    print(json.dumps({
-        "workload": "o64v512: o=64 as 2x32, v=512 as 8x64, seed 2",
-        "mixed_tuples": int(len(batch)), "mixed_flops": fl_batch, "mixed_kernel_s": ms_batch / 1e3,
-        "mixed_tflops": ach, "mixed_frac_of_bf16_peak": ach / bf16[0], "bf16_peak": bf16[0],
-        "fp64_one_tuple_tflops": fl_one / (fs_one / 1e3) / 1e12,
-        "mixed_one_tuple_tflops": fl_one / (ms_one / 1e3) / 1e12,
-        "one_tuple": [int(x) for x in one[0, :6]],
-        "E_fp64_one_tuple": list(f_one), "E_mixed_one_tuple": list(m_one),
-        "rel_err_E": max(abs(m_one[0] - f_one[0]) / abs(f_one[0]), abs(m_one[1] - f_one[1]) / abs(f_one[1])),
-        "E_mixed_batch": list(mixed), "device_bytes": dev_bytes, "input_generation_s": gen_s}), flush=True)
+        out["fp64_one_tuple"] = {"E": list(f_one), "tflops": fl_one / job.last_kernel_ms / 1e9}
+        for form, prec in MIXED_FORMS:
+            job.run(one, stream=stream, precision=prec)
+            m_one = job.run(one, stream=stream, precision=prec)
+            ms_one = job.last_kernel_ms
+            m_b = job.run(batch, stream=stream, precision=prec)
+            ms_b = job.last_kernel_ms
+            ach = fl_batch / ms_b / 1e9
+            out[form] = {"batch_tflops": ach, "batch_kernel_s": ms_b / 1e3, "frac_of_bf16_peak": ach / bf16[0],
+                         "one_tuple_tflops": fl_one / ms_one / 1e9, "E_one_tuple": list(m_one),
+                         "rel_err_ET": (m_one[0] - f_one[0]) / abs(f_one[0]),
+                         "rel_err_ETT": (m_one[1] - f_one[1]) / abs(f_one[1]),
+                         "rel_err_EST": ((m_one[1] - m_one[0]) - (f_one[1] - f_one[0])) / abs(f_one[1] - f_one[0]),
+                         "E_batch": list(m_b)}
+        out["device_bytes"] = job.device_bytes
+    print(json.dumps(out), flush=True)
 
 
 def main() -> None:
@@ -396,7 +414,10 @@ def main() -> None:
     ap.add_argument("--profile", action="store_true", help="small single-launch case for ncu")
     ap.add_argument("--tuples", type=int, default=2, help="tuples in the --profile case")
     ap.add_argument("--workload", default="o40v300", choices=["o40v300", "o64v512"])
-    ap.add_argument("--mixed", action="store_true", help="--profile case in the mixed form")
+    ap.add_argument("--case", default="o40v114", choices=["o40v114", "o64v128"], help="--profile case")
+    ap.add_argument("--kseg", type=int, default=0, help="mixed form: K chunks per accumulator drain")
+    ap.add_argument("--mixed", default="", choices=["", "tf32", "bf16", "fp16"],
+                    help="--profile case in a mixed form")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be at least 3")

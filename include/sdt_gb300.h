@@ -228,6 +228,10 @@ int64_t sdt_job_device_bytes(const sdt_job *job);
  * chains reduce the FP32 rounding of the split products at the cost of more
  * drains. */
 int sdt_job_set_mixed_segment(sdt_job *job, int chunks);
+/* Mixed form: run the kernel in clusters of `ctas` CTAs (1, the default, or
+ * 4).  With 4, the CTAs of a cluster take sub-boxes that differ in the j and
+ * k boxes and multicast the operand tiles they share. */
+int sdt_job_set_mixed_cluster(sdt_job *job, int ctas);
 /* When on, sdt_job_run brackets its fused-kernel launches with CUDA events
  * on the run's stream; sdt_job_last_kernel_ms returns that interval. */
 int sdt_job_set_timing(sdt_job *job, int on);

@@ -57,6 +57,7 @@ def _declare(lib):
         "sdt_launch_count": (I64, []),
         "sdt_job_set_timing": (C.c_int, [C.c_void_p, C.c_int]),
         "sdt_job_set_mixed_segment": (C.c_int, [C.c_void_p, C.c_int]),
+        "sdt_job_set_mixed_cluster": (C.c_int, [C.c_void_p, C.c_int]),
         "sdt_job_last_kernel_ms": (C.c_double, [C.c_void_p]),
         "sdt_probe_fp64_tflops": (C.c_double, [C.c_int]),
         "sdt_tc_selftest": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]),

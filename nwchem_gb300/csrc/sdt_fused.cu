@@ -691,25 +691,28 @@ extern "C" int sdt_job_run(sdt_job *j, const int64_t *klist, int64_t n, int prec
     cudaStream_t st = stream ? (cudaStream_t)stream : lib_stream();
     const Tiling &t = j->t;
     const int64_t nt = t.noab + t.nvab;
-    std::vector<int64_t> pref(n + 1, 0);
+    std::vector<int64_t> pref(n + 1, 0), spref(n + 1, 0);
     std::vector<double> fac(n);
     for (int64_t q = 0; q < n; ++q) {
         const int64_t *k = klist + 7 * q;
-        int64_t boxes = 1;
+        int64_t boxes = 1, supers = 1;  // mixed form: clusters of 4 take (j,k) box pairs
         for (int d = 0; d < 6; ++d) {
             const bool virt = d < 3;
             if (k[d] < 1 || k[d] > nt || (virt ? k[d] <= t.noab : k[d] > t.noab))
                 return fail(SDT_ERR_ARG, "sdt_job_run: tuple tile out of range");
             const int bx = virt ? box_v : box_o;
-            boxes *= (t.r(k[d]) + bx - 1) / bx;
+            const int64_t nb = (t.r(k[d]) + bx - 1) / bx;
+            boxes *= nb;
+            supers *= (d >= 4 && j->mixed_cluster == 4) ? (nb + 1) / 2 : nb;
         }
+        spref[q + 1] = spref[q] + supers;
         if (!(k[0] <= k[1] && k[1] <= k[2] && k[3] <= k[4] && k[4] <= k[5]))
             return fail(SDT_ERR_ARG, "sdt_job_run: tuple tiles not sorted");
         pref[q + 1] = pref[q] + boxes;
         fac[q] = tuple_factor(k, t.restricted != 0);
     }
     const int64_t items = pref[n];
-    void *p0 = j->klist_d, *p1 = j->pref_d, *p2 = j->factor_d, *p3 = j->task_d, *p4 = j->part_d;
+    void *p0 = j->klist_d, *p1 = j->pref_d, *p2 = j->factor_d, *p3 = j->task_d, *p4 = j->part_d, *p5 = j->spref_d;
     size_t c_tasks = j->cap_tasks, c_items = j->cap_items;
     // Workspace sized by the largest request so far.
     if (c_tasks < (size_t)n || !p0) {
@@ -718,6 +721,7 @@ extern "C" int sdt_job_run(sdt_job *j, const int64_t *klist, int64_t n, int prec
         cap = 0; ok = ok && grow(&p1, &cap, (n + 1) * sizeof(int64_t));
         cap = 0; ok = ok && grow(&p2, &cap, n * sizeof(double));
         cap = 0; ok = ok && grow(&p3, &cap, 2 * n * sizeof(double));
+        cap = 0; ok = ok && grow(&p5, &cap, (n + 1) * sizeof(int64_t));
         if (!ok) return fail(SDT_ERR_NOMEM, "sdt_job_run: workspace");
         c_tasks = n;
     }
@@ -727,7 +731,7 @@ extern "C" int sdt_job_run(sdt_job *j, const int64_t *klist, int64_t n, int prec
         c_items = items;
     }
     j->klist_d = (int64_t *)p0; j->pref_d = (int64_t *)p1; j->factor_d = (double *)p2;
-    j->task_d = (double *)p3; j->part_d = (double *)p4;
+    j->task_d = (double *)p3; j->part_d = (double *)p4; j->spref_d = (int64_t *)p5;
     j->cap_tasks = c_tasks; j->cap_items = c_items;
     if (!j->out_d) j->out_d = (double *)gpu_get(2 * sizeof(double));
     const size_t hbytes = (2 * n + 2) * sizeof(double);
@@ -741,6 +745,8 @@ extern "C" int sdt_job_run(sdt_job *j, const int64_t *klist, int64_t n, int prec
     int rc = cuda_check(cudaMemcpyAsync(j->klist_d, klist, 7 * n * sizeof(int64_t), cudaMemcpyHostToDevice, st), "sdt_job_run");
     if (!rc) rc = cuda_check(cudaMemcpyAsync(j->pref_d, pref.data(), (n + 1) * sizeof(int64_t), cudaMemcpyHostToDevice, st), "sdt_job_run");
     if (!rc) rc = cuda_check(cudaMemcpyAsync(j->factor_d, fac.data(), n * sizeof(double), cudaMemcpyHostToDevice, st), "sdt_job_run");
+    if (!rc && mixed)
+        rc = cuda_check(cudaMemcpyAsync(j->spref_d, spref.data(), (n + 1) * sizeof(int64_t), cudaMemcpyHostToDevice, st), "sdt_job_run");
     if (rc) return rc;
 
     if (mixed) {
@@ -753,7 +759,7 @@ extern "C" int sdt_job_run(sdt_job *j, const int64_t *klist, int64_t n, int prec
             if (!j->ev1) cudaEventCreate(&j->ev1);
             cudaEventRecord(j->ev0, st);
         }
-        rc = mixed_launch(j, items, n, st);
+        rc = mixed_launch(j, spref[n], n, st);
         if (j->timing) cudaEventRecord(j->ev1, st);
         if (rc) return rc;
     } else {
@@ -812,6 +818,7 @@ extern "C" int sdt_job_destroy(sdt_job *j) {
     gpu_put(j->pair_off);
     gpu_put(j->klist_d);
     gpu_put(j->pref_d);
+    gpu_put(j->spref_d);
     gpu_put(j->factor_d);
     gpu_put(j->part_d);
     gpu_put(j->task_d);
@@ -851,6 +858,12 @@ extern "C" int sdt_job_set_timing(sdt_job *j, int on) {
 }
 
 extern "C" double sdt_job_last_kernel_ms(const sdt_job *j) { return j ? (double)j->last_ms : -1.0; }
+
+extern "C" int sdt_job_set_mixed_cluster(sdt_job *j, int ctas) {
+    if (!j || (ctas != 1 && ctas != 4)) return fail(SDT_ERR_ARG, "sdt_job_set_mixed_cluster: 1 or 4 CTAs");
+    j->mixed_cluster = ctas;
+    return SDT_OK;
+}
 
 extern "C" int sdt_job_set_mixed_segment(sdt_job *j, int chunks) {
     if (!j || chunks < 0) return fail(SDT_ERR_ARG, "sdt_job_set_mixed_segment: bad argument");

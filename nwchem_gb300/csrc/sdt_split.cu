@@ -4,9 +4,21 @@
 // the latter overlapped with the next sub-box's contractions.
 //
 // Work unit (item): an 8x8x8 (a,b,c) x 4x4x4 (i,j,k) sub-box of one tuple's
-// triples tile, 32768 values.  Items are dealt to the CTAs round-robin (one
-// CTA per SM; item = blockIdx.x + n * gridDim.x), so results do not depend on
-// timing.
+// triples tile, 32768 values.  The kernel runs in clusters of 4 CTAs (one CTA
+// per SM) that take the 4 items of a "super-item" -- the same (a,b,c,i)
+// boxes, j boxes 2J+rj and k boxes 2K+rk (rj, rk in {0,1}, cluster rank
+// 2*rj+rk).  Super-items are dealt to the clusters round-robin
+// (super = cluster id + n * clusters), so results do not depend on timing.
+//
+// Operand sharing.  A merged term's A operand depends on its two row holes
+// and its B operand on its column hole.  Inside a cluster, an operand that
+// does not involve j or k is the same for all 4 CTAs, one that involves only
+// k (or only j) is the same for the 2 CTAs with the same rk (rj): each CTA
+// loads its quarter or half of every shared tile and multicasts it to the
+// CTAs that share it (TMA .multicast::cluster), so every CTA receives full
+// tiles while the L2 serves half the bytes.  A stage is refilled only after
+// all 4 CTAs' MMAs have released it (their tcgen05.commit arrives on the
+// stage's empty barrier in every CTA of the cluster).
 //
 // Contractions.  Every d1 term has exactly the row/column index layout and the
 // sign of one d2 term (d1_1/d2_8, d1_2/d2_9, d1_3/d2_7, d1_4/d2_2, d1_5/d2_3,
@@ -57,10 +69,10 @@ constexpr int SX_THREADS = 512;
 constexpr int SX_DRAIN = 128;                 // drain threads (warps 4-7)
 constexpr int SX_EPI = 256;                   // energy threads (warps 8-15)
 // Register split (setmaxnreg): the launch gives 128 per thread (4 warps per
-// SM sub-partition); warps 0-3 drop to 40, the drain warps to 88 and the
-// energy warps rise to 192: 128*40 + 128*88 + 256*192 = 65536 = 512*128, and each
-// sub-partition holds one warp of each group: (40+88+2*192)*32 = 16384.
-constexpr int SX_REG_LAUNCH = 128, SX_REG_LOW = 40, SX_REG_DRAIN = 88, SX_REG_HIGH = 192;
+// SM sub-partition); warps 0-3 drop to 56, the drain warps to 72 and the
+// energy warps rise to 192: 128*56 + 128*72 + 256*192 = 65536 = 512*128, and
+// each sub-partition holds one warp of each group: (56+72+2*192)*32 = 16384.
+constexpr int SX_REG_LAUNCH = 128, SX_REG_LOW = 56, SX_REG_DRAIN = 72, SX_REG_HIGH = 192;
 static_assert(128 * SX_REG_LOW + 128 * SX_REG_DRAIN + 256 * SX_REG_HIGH <= SX_THREADS * SX_REG_LAUNCH,
               "register split");
 // setmaxnreg.dec may only lower and setmaxnreg.inc only raise a warp's count.
@@ -107,49 +119,84 @@ struct EDesc {
     long long item;
 };
 
+// Split operands live in HBM "block-major": one block per (row boxes, K chunk)
+// holds a whole stage tile -- 128 rows (A) or 256 rows (B) of 32 bytes, in the
+// row order the MMA reads and already 32-byte swizzled -- so a stage is four
+// contiguous bulk copies (A hi/lo 4 KB, B hi/lo 8 KB).  Rows are the box
+// products of the tiles' boxes (8 particle or 4 hole indices, zero padded
+// at tile ends); box ids are global over all tiles of a space.
+//   Wd1 (d1 A)  [X][H1][H2][kc_o]   rows (R0 8, R1 4, R2 4), K = m
+//   T2b (d2 A)  [X][H1][H2][kc_v]   rows (R0 8, R1 4, R2 4), K = e
+//   T2a (d1 B)  [X0][X1][H][kc_o]   rows (C0 8, C1 8, C2 4), K = m
+//   Vd2 (d2 B)  per tile pair (B<=C): [lb0][lb1][H][kc_v], lb local boxes
+enum { L_WD1 = 0, L_T2B, L_T2A, L_VD2, L_N };
+
 struct SplitParams {
-    CUtensorMap t2b_hi, t2b_lo, t2a_hi, t2a_lo, wd1_hi, wd1_lo;
-    const CUtensorMap *vd2_maps;  // [2*pair]: hi, lo
-    const int32_t *pair_id;       // [nvab*nvab]
+    const uint8_t *blk[2 * L_N];  // [2*layout + (0 hi, 1 lo)]
+    const int32_t *tile_box;      // [ntiles]: global box id of the tile's first box (its space)
+    const int64_t *pair_blk;      // [nvab*nvab]: first Vd2 block of tile pair (B<=C), -1 none
     const float *T1f, *Uf;        // FP32 copies: [v][o], [v][v][o][o]
     const double *evl;
     const int32_t *tiles;         // [ntiles][4] start, range, spin, sym
-    int32_t noab, nvab, nk_o, nk_v, kseg;
+    int32_t noab, nvab, nk_o, nk_v, kseg, nob, nvb;
     int64_t nocc, nvir;
-    const int64_t *klist, *item_pref;
+    const int64_t *klist, *item_pref, *super_pref;
     const double *factor;
-    int64_t n_tasks, items;
+    int64_t n_tasks, n_super;
     double inv_s, inv_s2;         // undo the operand scaling (FP16): X_true = X * inv_s
     double *part;
     int *err;
 };
 
 struct ItemBox {
-    int tile[6], start[6], ext[6], boff[6];
-    int64_t tq;
+    int tile[6], start[6], ext[6], boff[6], lbox[6];  // lbox: local box, clamped into the tile
+    int64_t tq, item;  // item = -1: this CTA's box lies outside the tuple
 };
 
-__device__ __forceinline__ void decode_item(const SplitParams &p, int64_t item, ItemBox &b) {
+// Decodes work unit si.  PJ = 2 (clusters of 4): the unit is a super-item and
+// this CTA takes j box 2J+rj and k box 2K+rk; PJ = 1: the unit is one item.
+template <int PJ>
+__device__ __forceinline__ void decode_super(const SplitParams &p, int64_t si, int rj, int rk, ItemBox &b) {
     int64_t lo = 0, hi = p.n_tasks - 1;
     while (lo < hi) {
         const int64_t mid = (lo + hi + 1) >> 1;
-        if (p.item_pref[mid] <= item) lo = mid;
+        if (p.super_pref[mid] <= si) lo = mid;
         else hi = mid - 1;
     }
     b.tq = lo;
-    int64_t local = item - p.item_pref[lo];
+    int64_t local = si - p.super_pref[lo];
+    int nb[6];
 #pragma unroll
     for (int d = 0; d < 6; ++d) {
         b.tile[d] = (int)p.klist[7 * lo + d];
         b.start[d] = __ldg(p.tiles + 4 * (b.tile[d] - 1));
         b.ext[d] = __ldg(p.tiles + 4 * (b.tile[d] - 1) + 1);
+        const int bx = d < 3 ? SX_BV : SX_BO;
+        nb[d] = (b.ext[d] + bx - 1) / bx;
+    }
+    int box[6];
+    const int nk2 = (nb[5] + PJ - 1) / PJ, nj2 = (nb[4] + PJ - 1) / PJ;
+    box[5] = PJ * (int)(local % nk2) + rk;
+    local /= nk2;
+    box[4] = PJ * (int)(local % nj2) + rj;
+    local /= nj2;
+#pragma unroll
+    for (int d = 3; d >= 0; --d) {
+        box[d] = (int)(local % nb[d]);
+        local /= nb[d];
     }
 #pragma unroll
-    for (int d = 5; d >= 0; --d) {
-        const int bx = d < 3 ? SX_BV : SX_BO;
-        const int nb = (b.ext[d] + bx - 1) / bx;
-        b.boff[d] = (int)(local % nb) * bx;
-        local /= nb;
+    for (int d = 0; d < 6; ++d) {
+        b.boff[d] = box[d] * (d < 3 ? SX_BV : SX_BO);
+        b.lbox[d] = min(box[d], nb[d] - 1);
+    }
+    if (box[4] < nb[4] && box[5] < nb[5]) {
+        int64_t x = box[0];
+#pragma unroll
+        for (int d = 1; d < 6; ++d) x = x * nb[d] + box[d];
+        b.item = p.item_pref[lo] + x;
+    } else {
+        b.item = -1;
     }
 }
 
@@ -163,31 +210,64 @@ __device__ __forceinline__ void mma_split(uint32_t d, uint64_t a, uint64_t b, ui
     else tc::mma_f16(d, a, b, tc::idesc_f16(128, 256, TYPE == TM_BF16), acc);
 }
 
+__device__ __forceinline__ void bulk_load(void *dst, const void *src, uint32_t bytes, uint64_t *bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                 ::"r"(tc::smem_u32(dst)), "l"(src), "r"(bytes), "r"(tc::smem_u32(bar))
+                 : "memory");
+}
+__device__ __forceinline__ void bulk_load_mc(void *dst, const void *src, uint32_t bytes, uint64_t *bar,
+                                             uint16_t mask) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes.multicast::cluster [%0], [%1], %2, [%3], %4;"
+        ::"r"(tc::smem_u32(dst)), "l"(src), "r"(bytes), "r"(tc::smem_u32(bar)), "h"(mask)
+        : "memory");
+}
+
 // ---------------------------------------------------------------------------
-// TMA producer (one thread).
-template <int TYPE>
+// Operand producer (one thread): per stage, the A and B blocks (hi, lo) of
+// the term's K chunk.  With clusters of 4 (CS = 4), per merged term and rank
+// (rj, rk):
+//   rows (x;j,k) [terms 0,3,6]: A own;  B shared by all 4: quarter `rank`;
+//   rows (x;i,k) [terms 1,4,7]: A shared by the two CTAs with this rk: half rj;
+//       B (column hole j) shared by the two with this rj: half rk;
+//   rows (x;i,j) [terms 2,5,8]: A shared by the two with this rj: half rk;
+//       B (column hole k) shared by the two with this rk: half rj;
+// each piece is multicast to the CTAs that share it.  Halves and quarters
+// split the slowest row index (R0 of A, C0 of B): contiguous runs of a block.
+template <int TYPE, int CS>
 __device__ __forceinline__ void run_producer(const SplitParams &p, uint8_t *stages, uint64_t *full,
-                                             uint64_t *empty, volatile int *abort) {
-    constexpr int KE = TYPE == TM_F32 ? 8 : 16;  // K elements per 32-byte row
+                                             uint64_t *empty, volatile int *abort, int rj, int rk,
+                                             int64_t unit0, int64_t ustep) {
+    constexpr int PJ = CS == 4 ? 2 : 1;
     const int nk = p.nk_o + p.nk_v;
-    tc::prefetch_tmap(&p.t2b_hi);
-    tc::prefetch_tmap(&p.t2a_hi);
-    tc::prefetch_tmap(&p.wd1_hi);
+    const int rank = 2 * rj + rk;
+    const uint16_t m_all = 0xF, m_rk = (uint16_t)((1u << rk) | (1u << (2 + rk))), m_rj = (uint16_t)(3u << (2 * rj));
+    const int64_t NOB = p.nob, NVB = p.nvb;
     uint32_t g = 0;
     bool stop = false;
-    for (int64_t it = blockIdx.x; it < p.items && !stop; it += gridDim.x) {
+    for (int64_t si = unit0; si < p.n_super && !stop; si += ustep) {
         ItemBox bx;
-        decode_item(p, it, bx);
-        int gs[6];
+        decode_super<PJ>(p, si, rj, rk, bx);
+        int gb[6];  // global box ids
 #pragma unroll
-        for (int d = 0; d < 6; ++d) gs[d] = bx.start[d] + bx.boff[d];
+        for (int d = 0; d < 6; ++d) gb[d] = __ldg(p.tile_box + bx.tile[d] - 1) + bx.lbox[d];
         for (int t = 0; t < 9 && !stop; ++t) {
             const MergedTerm td = kMerged[t];
-            const int gr0 = gs[td.r[0]], gr1 = gs[td.r[1]], gr2 = gs[td.r[2]];
-            const int gc0 = gs[td.c[0]], gc1 = gs[td.c[1]], gc2 = gs[td.c[2]];
-            const int pr = p.pair_id[(bx.tile[td.c[0]] - p.noab - 1) * p.nvab + (bx.tile[td.c[1]] - p.noab - 1)];
-            const CUtensorMap *vh = p.vd2_maps + 2 * pr, *vl = vh + 1;
-            const int vb1 = bx.boff[td.c[1]], vb0 = bx.boff[td.c[0]];
+            const int ty = t % 3;
+            // first blocks of the term's d1 and d2 parts (K chunk 0)
+            const int64_t arow = ((int64_t)gb[td.r[0]] * NOB + gb[td.r[1]]) * NOB + gb[td.r[2]];
+            const int64_t a1 = arow * p.nk_o, a2 = arow * p.nk_v;
+            const int64_t b1 = (((int64_t)gb[td.c[0]] * NVB + gb[td.c[1]]) * NOB + gb[td.c[2]]) * p.nk_o;
+            const int tc1 = bx.tile[td.c[1]];
+            const int nbc1 = (__ldg(p.tiles + 4 * (tc1 - 1) + 1) + SX_BV - 1) / SX_BV;
+            const int64_t b2 = __ldg(p.pair_blk + (bx.tile[td.c[0]] - p.noab - 1) * p.nvab + (tc1 - p.noab - 1)) +
+                               (((int64_t)bx.lbox[td.c[0]] * nbc1 + bx.lbox[td.c[1]]) * NOB + gb[td.c[2]]) * p.nk_v;
+            // this CTA's piece of A (ha < 0: whole) and of B (piece hb of nbp)
+            const int ha = (CS == 1 || ty == 0) ? -1 : ty == 1 ? rj : rk;
+            const uint16_t ma = ty == 1 ? m_rk : m_rj;
+            const int nbp = CS == 1 ? 1 : ty == 0 ? 4 : 2;
+            const int hb = CS == 1 ? 0 : ty == 0 ? rank : ty == 1 ? rk : rj;
+            const uint16_t mb = ty == 0 ? m_all : ty == 1 ? m_rj : m_rk;
             for (int kc = 0; kc < nk; ++kc, ++g) {
                 const int s = g % SX_NS;
                 if (g >= SX_NS && !tc::mbar_wait(&empty[s], ((g / SX_NS) & 1) ^ 1, kWaitNs, abort)) {
@@ -195,19 +275,28 @@ __device__ __forceinline__ void run_producer(const SplitParams &p, uint8_t *stag
                     break;
                 }
                 uint8_t *st = stages + s * SX_STAGE;
-                tc::mbar_arrive_expect_tx(&full[s], SX_STAGE);
-                if (kc < p.nk_o) {  // d1 part: A = w(m,R0,R1,R2), B = t(C0,C1;C2,m)
-                    const int k0 = kc * KE;
-                    tc::tma_load_4d(st, &p.wd1_hi, &full[s], k0, gr2, gr1, gr0);
-                    tc::tma_load_4d(st + SX_A, &p.wd1_lo, &full[s], k0, gr2, gr1, gr0);
-                    tc::tma_load_4d(st + 2 * SX_A, &p.t2a_hi, &full[s], k0, gc2, gc1, gc0);
-                    tc::tma_load_4d(st + 2 * SX_A + SX_B, &p.t2a_lo, &full[s], k0, gc2, gc1, gc0);
-                } else {  // d2 part: A = t(R0,e;R1,R2), B = v(C0,C1,C2,e)
-                    const int k0 = (kc - p.nk_o) * KE;
-                    tc::tma_load_4d(st, &p.t2b_hi, &full[s], k0, gr2, gr1, gr0);
-                    tc::tma_load_4d(st + SX_A, &p.t2b_lo, &full[s], k0, gr2, gr1, gr0);
-                    tc::tma_load_4d(st + 2 * SX_A, vh, &full[s], k0, gc2, vb1, vb0);
-                    tc::tma_load_4d(st + 2 * SX_A + SX_B, vl, &full[s], k0, gc2, vb1, vb0);
+                tc::mbar_arrive_expect_tx(&full[s], SX_STAGE);  // this CTA's whole stage, from all issuers
+                const bool d1 = kc < p.nk_o;
+                const int la = d1 ? L_WD1 : L_T2B, lb = d1 ? L_T2A : L_VD2;
+                const int64_t ab = d1 ? a1 + kc : a2 + (kc - p.nk_o);
+                const int64_t bb = d1 ? b1 + kc : b2 + (kc - p.nk_o);
+                const uint8_t *ah = p.blk[2 * la] + ab * SX_A, *al = p.blk[2 * la + 1] + ab * SX_A;
+                const uint8_t *bh = p.blk[2 * lb] + bb * SX_B, *bl = p.blk[2 * lb + 1] + bb * SX_B;
+                if (ha < 0) {
+                    bulk_load(st, ah, SX_A, &full[s]);
+                    bulk_load(st + SX_A, al, SX_A, &full[s]);
+                } else {
+                    const int off = ha * (SX_A / 2);
+                    bulk_load_mc(st + off, ah + off, SX_A / 2, &full[s], ma);
+                    bulk_load_mc(st + SX_A + off, al + off, SX_A / 2, &full[s], ma);
+                }
+                if (nbp == 1) {
+                    bulk_load(st + 2 * SX_A, bh, SX_B, &full[s]);
+                    bulk_load(st + 2 * SX_A + SX_B, bl, SX_B, &full[s]);
+                } else {
+                    const int piece = SX_B / nbp, off = hb * piece;
+                    bulk_load_mc(st + 2 * SX_A + off, bh + off, piece, &full[s], mb);
+                    bulk_load_mc(st + 2 * SX_A + SX_B + off, bl + off, piece, &full[s], mb);
                 }
             }
         }
@@ -224,16 +313,16 @@ __device__ __forceinline__ void run_producer(const SplitParams &p, uint8_t *stag
 
 // ---------------------------------------------------------------------------
 // MMA issuer (one thread).
-template <int TYPE>
+template <int TYPE, int CS>
 __device__ __forceinline__ void run_mma(const SplitParams &p, uint8_t *stages, uint64_t *full, uint64_t *empty,
                                         uint64_t *tfull, uint64_t *tempty, uint64_t *drain, uint32_t tmem,
-                                        volatile int *abort) {
+                                        volatile int *abort, int64_t unit0, int64_t ustep) {
     const int nk = p.nk_o + p.nk_v;
     const int kseg = p.kseg > 0 && p.kseg < nk ? p.kseg : nk;
     const int nseg = (nk + kseg - 1) / kseg;
     uint32_t g = 0, sg = 0;  // stage and segment counters
     bool stop = false;
-    for (int64_t it = blockIdx.x; it < p.items && !stop; it += gridDim.x) {
+    for (int64_t si = unit0; si < p.n_super && !stop; si += ustep) {
         for (int t = 0; t < 9 && !stop; ++t) {
             for (int sgi = 0; sgi < nseg && !stop; ++sgi, ++sg) {
                 const int buf = sg & 1;
@@ -257,7 +346,8 @@ __device__ __forceinline__ void run_mma(const SplitParams &p, uint8_t *stages, u
                     mma_split<TYPE>(d_tmem, ah, bh, kc == sgi * kseg ? 0u : 1u);
                     mma_split<TYPE>(d_tmem, ah, bl, 1u);
                     mma_split<TYPE>(d_tmem, al, bh, 1u);
-                    tc::mma_commit(&empty[s]);
+                    if (CS == 4) tc::mma_commit_mc(&empty[s], 0xF);  // free here: tell all 4 CTAs
+                    else tc::mma_commit(&empty[s]);
                 }
                 if (!stop) tc::mma_commit(&tfull[buf]);
             }
@@ -322,6 +412,21 @@ __device__ __forceinline__ void drain_any(int t, bool store, float *X, uint32_t 
     }
 }
 
+// Exact FP32 -> FP64 widening by assembling the IEEE-754 fields on the
+// integer pipes (the conversion instruction runs on the FP64 pipe, which
+// bounds the energy pass): sign kept, exponent rebiased by 1023 - 127,
+// mantissa shifted into the top 23 of 52 bits; zero and FP32 subnormals
+// (|x| < 2^-126) give signed zero, infinities and NaNs keep their class.
+__device__ __forceinline__ double widen(float f) {
+    const uint32_t u = __float_as_uint(f);
+    const uint32_t e = (u >> 23) & 0xffu;
+    const uint32_t m = u & 0x7fffffu;
+    const uint32_t e64 = e == 0xffu ? 0x7ffu : e + 896u;
+    const uint32_t hi = (u & 0x80000000u) | (e ? (e64 << 20) | (m >> 3) : 0u);
+    const uint32_t lo = e ? (m << 29) : 0u;
+    return __hiloint2double((int)hi, (int)lo);
+}
+
 // ---------------------------------------------------------------------------
 // Energies of one item from its values R in registers: thread (b;i,j) with
 // R[32*A + 4*c + k] = X(a = 4*half + A, b, c, i, j, k).
@@ -343,6 +448,9 @@ __device__ __forceinline__ void energy_chunk(const float (&R)[128], const EDesc 
     const double *__restrict__ ev = p.evl + p.nocc;
     const double eij = __ldg(eo + gi) + __ldg(eo + gj);
     const double eab = __ldg(ev + ga) + __ldg(ev + gb);
+    double P[4];  // e_i + e_j + e_k
+#pragma unroll
+    for (int k = 0; k < 4; ++k) P[k] = k < nk ? eij + __ldg(eo + gk0 + k) : 0.0;
     const float *__restrict__ t1a = p.T1f + (int64_t)ga * o;
     const float *__restrict__ t1b = p.T1f + (int64_t)gb * o;
     const float t1ai = __ldg(t1a + gi), t1aj = __ldg(t1a + gj), t1bi = __ldg(t1b + gi), t1bj = __ldg(t1b + gj);
@@ -371,11 +479,11 @@ __device__ __forceinline__ void energy_chunk(const float (&R)[128], const EDesc 
                     s = fmaf(t1ci, __ldg(uab + gj * o + gk), s);
                     s = fmaf(-t1cj, __ldg(uab + gi * o + gk), s);
                     s = fmaf(__ldg(t1c + gk), uabij, s);
-                    const double x = (double)R[A * 32 + c * 4 + k];
-                    const double D = (eij + __ldg(eo + gk)) - Q;
+                    const double x = widen(R[A * 32 + c * 4 + k]);
+                    const double D = P[k] - Q;
                     const double q = div_nr(x, D);
                     e1 = fma(q, x, e1);
-                    est = fma(q, (double)s, est);
+                    est = fma(q, widen(s), est);
                 }
             }
         }
@@ -405,8 +513,9 @@ __device__ __forceinline__ void write_partial(double &e1, double &est, double *r
     est = 0.0;
 }
 
-template <int TYPE>
+template <int TYPE, int CS>
 __global__ void __launch_bounds__(SX_THREADS, 1) split_fused_kernel(const __grid_constant__ SplitParams p) {
+    constexpr int PJ = CS == 4 ? 2 : 1;
     extern __shared__ __align__(1024) uint8_t smem_raw[];
     uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     float *X = (float *)smem;
@@ -426,7 +535,7 @@ __global__ void __launch_bounds__(SX_THREADS, 1) split_fused_kernel(const __grid
     if (threadIdx.x == 0) {
         for (int s = 0; s < SX_NS; ++s) {
             tc::mbar_init(&full[s], 1);
-            tc::mbar_init(&empty[s], 1);
+            tc::mbar_init(&empty[s], CS);  // one release from each CTA of the cluster
         }
         for (int s = 0; s < 2; ++s) {
             tc::mbar_init(&tfull[s], 1);
@@ -444,15 +553,22 @@ __global__ void __launch_bounds__(SX_THREADS, 1) split_fused_kernel(const __grid
     tc::tc_fence_before();
     __syncthreads();
     tc::tc_fence_after();
+    // every CTA's barriers exist before any peer multicasts into them
+    if (CS > 1) tc::cluster_sync();
     const uint32_t tmem = *tslot;
+    const int rank = CS > 1 ? (int)tc::cluster_rank() : 0;
+    const int rj = rank >> 1, rk = rank & 1;
+    const int64_t unit0 = CS > 1 ? tc::cluster_id_x() : blockIdx.x;
+    const int64_t ustep = CS > 1 ? tc::cluster_count_x() : gridDim.x;
 
     const int nk = p.nk_o + p.nk_v;
     const int kseg = p.kseg > 0 && p.kseg < nk ? p.kseg : nk;
     const int nseg = (nk + kseg - 1) / kseg;
     if (warp < 4) {
         asm volatile("setmaxnreg.dec.sync.aligned.u32 %0;" ::"n"(SX_REG_LOW));
-        if (warp == 0 && lane == 0) run_producer<TYPE>(p, stages, full, empty, abort);
-        else if (warp == 1 && lane == 0) run_mma<TYPE>(p, stages, full, empty, tfull, tempty, drain, tmem, abort);
+        if (warp == 0 && lane == 0) run_producer<TYPE, CS>(p, stages, full, empty, abort, rj, rk, unit0, ustep);
+        else if (warp == 1 && lane == 0)
+            run_mma<TYPE, CS>(p, stages, full, empty, tfull, tempty, drain, tmem, abort, unit0, ustep);
     } else if (warp < 8) {
         // ---------------- drain warps ----------------
         asm volatile("setmaxnreg.dec.sync.aligned.u32 %0;" ::"n"(SX_REG_DRAIN));
@@ -463,7 +579,7 @@ __global__ void __launch_bounds__(SX_THREADS, 1) split_fused_kernel(const __grid
         uint32_t sg = 0;
         int n = 0;  // items started by this CTA
         bool ok = true;
-        for (int64_t it = blockIdx.x; it < p.items && ok; it += gridDim.x, ++n) {
+        for (int64_t si = unit0; si < p.n_super && ok; si += ustep, ++n) {
             for (int t = 0; t < 9 && ok; ++t) {
                 for (int sgi = 0; sgi < nseg; ++sgi, ++sg) {
                     const int buf = sg & 1;
@@ -499,26 +615,26 @@ __global__ void __launch_bounds__(SX_THREADS, 1) split_fused_kernel(const __grid
         asm volatile("setmaxnreg.inc.sync.aligned.u32 %0;" ::"n"(SX_REG_HIGH));
         const int et = threadIdx.x - 256;
         const int mm = et & 127, half = et >> 7;
-        const int rb = mm >> 4, ri = (mm >> 2) & 3, rj = mm & 3;  // thread row (b;i,j)
+        const int rb = mm >> 4, ri = (mm >> 2) & 3, rj_ = mm & 3;  // thread row (b;i,j)
         const int ew = et >> 5;
         const bool leader = (et == 0);
         float R[128];
         double e1 = 0.0, est = 0.0;
         int n = 0;
-        for (int64_t it = blockIdx.x; it < p.items; it += gridDim.x, ++n) {
+        for (int64_t si = unit0; si < p.n_super; si += ustep, ++n) {
             if (leader) {
                 const bool w = tc::mbar_wait(xready, n & 1, kWaitNs, abort);
                 *en_ok = w ? 1 : 0;
                 if (w) {
                     ItemBox bx;
-                    decode_item(p, it, bx);
+                    decode_super<PJ>(p, si, rj, rk, bx);
 #pragma unroll
                     for (int dd = 0; dd < 6; ++dd) {
                         desc->g[dd] = bx.start[dd] + bx.boff[dd];
                         desc->nv[dd] = min(dd < 3 ? SX_BV : SX_BO, bx.ext[dd] - bx.boff[dd]);
                     }
                     desc->factor = p.factor[bx.tq];
-                    desc->item = it;
+                    desc->item = bx.item;
                 } else {
                     *abort = 1;
                     atomicCAS(p.err, 0, 4);
@@ -531,15 +647,17 @@ __global__ void __launch_bounds__(SX_THREADS, 1) split_fused_kernel(const __grid
 #pragma unroll
                 for (int c = 0; c < 8; ++c)
 #pragma unroll
-                    for (int k = 0; k < 4; ++k) R[A * 32 + c * 4 + k] = X[xaddr(4 * half + A, rb, c, ri, rj, k)];
+                    for (int k = 0; k < 4; ++k) R[A * 32 + c * 4 + k] = X[xaddr(4 * half + A, rb, c, ri, rj_, k)];
             named_bar(2, SX_EPI);
             if (leader) tc::mbar_arrive(xfree);
             const EDesc &d = *desc;
-            energy_chunk<0>(R, d, p, half, rb, ri, rj, e1, est);
-            energy_chunk<1>(R, d, p, half, rb, ri, rj, e1, est);
-            energy_chunk<2>(R, d, p, half, rb, ri, rj, e1, est);
-            energy_chunk<3>(R, d, p, half, rb, ri, rj, e1, est);
-            write_partial(e1, est, red, d, p, ew, lane, leader);
+            if (d.item >= 0) {  // a box outside the tuple has no item
+                energy_chunk<0>(R, d, p, half, rb, ri, rj_, e1, est);
+                energy_chunk<1>(R, d, p, half, rb, ri, rj_, e1, est);
+                energy_chunk<2>(R, d, p, half, rb, ri, rj_, e1, est);
+                energy_chunk<3>(R, d, p, half, rb, ri, rj_, e1, est);
+                write_partial(e1, est, red, d, p, ew, lane, leader);
+            }
         }
     }
     tc::tc_fence_before();
@@ -548,33 +666,106 @@ __global__ void __launch_bounds__(SX_THREADS, 1) split_fused_kernel(const __grid
         tc::tc_fence_after();
         tc::tmem_dealloc(tmem, 512);
     }
+    // no CTA leaves while peers may still multicast into it or arrive on its barriers
+    if (CS > 1) tc::cluster_sync();
 }
 
 // ---------------------------------------------------------------------------
 // Operand preparation.
 
-// FP64 rows [rows][n] -> split rows hi/lo [rows][n_pad] of element type TYPE
-// (zero padding), each value first multiplied by the power of two `scale`.
+struct PackArgs {
+    const double *src;
+    uint8_t *hi, *lo;
+    int64_t nblocks;
+    int layout, nk, ke, es;       // L_*, K chunks, K values per 32-byte row, bytes per value
+    int64_t o, v;
+    int nob, nvb;
+    const int32_t *vrow0, *vn;    // [nvb] first particle index and valid rows of each box
+    const int32_t *orow0, *on;    // [nob] the same for hole boxes
+    const int64_t *pblk0;         // Vd2: [npairs+1] first block of each tile pair, then the total
+    const int64_t *poff;          // Vd2: [npairs] FP64 offset of the pair's region
+    const int32_t *pdim;          // Vd2: [npairs][3] rB, rC, boxes of C
+    int npairs;
+    double scale;
+};
+
+// One thread per value of the block-major layout: gathers the FP64 source
+// (zero outside the tiles and past K), scales, splits into hi/lo of TYPE and
+// stores both at the 32-byte-swizzled position of its row (16-byte halves
+// swapped in rows with bit 2 set, the pattern of a 32-byte swizzled K-major
+// shared-memory tile).
 template <int TYPE>
-__global__ void __launch_bounds__(256) split_rows_kernel(const double *__restrict__ src, void *hi_, void *lo_,
-                                                         int64_t rows, int64_t n, int64_t n_pad, double scale) {
-    const int64_t total = rows * n_pad;
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total;
-         i += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t r = i / n_pad, c = i % n_pad;
-        const double x = c < n ? src[r * n + c] * scale : 0.0;
+__global__ void __launch_bounds__(256) pack_blocks_kernel(const PackArgs g) {
+    const int rows = (g.layout == L_WD1 || g.layout == L_T2B) ? 128 : 256;
+    const int64_t per_block = (int64_t)rows * g.ke;
+    const int64_t total = g.nblocks * per_block;
+    for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+         idx += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t blk = idx / per_block;
+        const int rem = (int)(idx - blk * per_block);
+        const int row = rem / g.ke, e = rem % g.ke;
+        int64_t q = blk;
+        const int kc = (int)(q % g.nk);
+        q /= g.nk;
+        const int kidx = kc * g.ke + e;
+        double x = 0.0;
+        if (g.layout == L_WD1 || g.layout == L_T2B) {
+            const int h2 = (int)(q % g.nob);
+            q /= g.nob;
+            const int h1 = (int)(q % g.nob);
+            const int xb = (int)(q / g.nob);
+            const int r0 = row >> 4, r1 = (row >> 2) & 3, r2 = row & 3;
+            const int64_t kext = g.layout == L_WD1 ? g.o : g.v;
+            if (r0 < g.vn[xb] && r1 < g.on[h1] && r2 < g.on[h2] && kidx < kext) {
+                const int64_t P = g.vrow0[xb] + r0, H = g.orow0[h1] + r1, L = g.orow0[h2] + r2;
+                x = g.src[((P * g.o + H) * g.o + L) * kext + kidx];  // Wd1[c][j][k][m], T2b[p][h][l][e]
+            }
+        } else if (g.layout == L_T2A) {
+            const int hb = (int)(q % g.nob);
+            q /= g.nob;
+            const int x1 = (int)(q % g.nvb);
+            const int x0 = (int)(q / g.nvb);
+            const int c0 = row >> 5, c1 = (row >> 2) & 7, c2 = row & 3;
+            if (c0 < g.vn[x0] && c1 < g.vn[x1] && c2 < g.on[hb] && kidx < g.o) {
+                const int64_t P = g.vrow0[x0] + c0, Q = g.vrow0[x1] + c1, H = g.orow0[hb] + c2;
+                x = g.src[((P * g.v + Q) * g.o + H) * g.o + kidx];  // T2a[p][q][h][m]
+            }
+        } else {
+            int lo = 0, hi = g.npairs - 1;
+            while (lo < hi) {
+                const int mid = (lo + hi + 1) >> 1;
+                if (g.pblk0[mid] <= blk) lo = mid;
+                else hi = mid - 1;
+            }
+            int64_t lq = blk - g.pblk0[lo];
+            lq /= g.nk;
+            const int hb = (int)(lq % g.nob);
+            lq /= g.nob;
+            const int rB = g.pdim[3 * lo], rC = g.pdim[3 * lo + 1], nbC = g.pdim[3 * lo + 2];
+            const int l1 = (int)(lq % nbC), l0 = (int)(lq / nbC);
+            const int c0 = row >> 5, c1 = (row >> 2) & 7, c2 = row & 3;
+            const int bl = 8 * l0 + c0, cl = 8 * l1 + c1;
+            if (bl < rB && cl < rC && c2 < g.on[hb] && kidx < g.v) {
+                const int64_t K = g.orow0[hb] + c2;
+                x = g.src[g.poff[lo] + (((int64_t)bl * rC + cl) * g.o + K) * g.v + kidx];  // region [b][c][k][e]
+            }
+        }
+        x *= g.scale;
+        const int eb = e * g.es;
+        const int off = row * 32 + ((((eb >> 4) ^ (row >> 2)) & 1) << 4) + (eb & 15);
+        const int64_t at = blk * (int64_t)rows * 32 + off;
         if (TYPE == TM_F32) {
             const float h = tc::to_tf32(__double2float_rn(x));
-            ((float *)hi_)[i] = h;
-            ((float *)lo_)[i] = tc::to_tf32(__double2float_rn(x - (double)h));
+            *(float *)(g.hi + at) = h;
+            *(float *)(g.lo + at) = tc::to_tf32(__double2float_rn(x - (double)h));
         } else if (TYPE == TM_BF16) {
             const __nv_bfloat16 h = __float2bfloat16_rn(__double2float_rn(x));
-            ((__nv_bfloat16 *)hi_)[i] = h;
-            ((__nv_bfloat16 *)lo_)[i] = __float2bfloat16_rn(__double2float_rn(x - (double)__bfloat162float(h)));
+            *(__nv_bfloat16 *)(g.hi + at) = h;
+            *(__nv_bfloat16 *)(g.lo + at) = __float2bfloat16_rn(__double2float_rn(x - (double)__bfloat162float(h)));
         } else {
             const __half h = __float2half_rn(__double2float_rn(x));
-            ((__half *)hi_)[i] = h;
-            ((__half *)lo_)[i] = __float2half_rn(__double2float_rn(x - (double)__half2float(h)));
+            *(__half *)(g.hi + at) = h;
+            *(__half *)(g.lo + at) = __float2half_rn(__double2float_rn(x - (double)__half2float(h)));
         }
     }
 }
@@ -620,13 +811,11 @@ void mixed_release(sdt_job *j) {
     }
     gpu_put(j->t1f);
     gpu_put(j->uf);
-    gpu_put(j->vd2_maps);
-    gpu_put(j->pair_id);
+    gpu_put(j->tile_box_d);
     gpu_put(j->err_d);
     host_put(j->err_h);
     j->t1f = j->uf = nullptr;
-    j->vd2_maps = nullptr;
-    j->pair_id = nullptr;
+    j->tile_box_d = nullptr;
     j->err_d = nullptr;
     j->err_h = nullptr;
     j->mixed_type = -1;
@@ -635,14 +824,10 @@ void mixed_release(sdt_job *j) {
 int mixed_prepare(sdt_job *j, int type, cudaStream_t st) {
     mixed_release(j);
     const Tiling &t = j->t;
-    const int64_t o = t.nocc, v = t.nvir, noab = t.noab, nvab = t.nvab;
+    const int64_t o = t.nocc, v = t.nvir, noab = t.noab, nvab = t.nvab, nt = noab + nvab;
     const int es = type == TM_F32 ? 4 : 2;
-    const int ke = 32 / es;                      // K elements per 32-byte row
-    const int64_t pad = 16 / es;                 // rows padded to 16-byte multiples
-    const int64_t op = (o + pad - 1) / pad * pad, vp = (v + pad - 1) / pad * pad;
-    j->o_pad = op;
-    j->v_pad = vp;
-    const int64_t vd2_elems = (int64_t)j->arr_n[DST_VD2];
+    const int ke = 32 / es;  // K values per 32-byte row
+    const int64_t nko = (o + ke - 1) / ke, nkv = (v + ke - 1) / ke;
     int rc = SDT_OK;
     // Power-of-two operand scales (FP16 only): s_T for T2, s_I for W and V,
     // so that every merged term accumulates s_T*s_I*X.
@@ -672,107 +857,129 @@ int mixed_prepare(sdt_job *j, int type, cudaStream_t st) {
     }
     j->inv_s = 1.0 / (sT * sI);
     j->inv_s2 = j->inv_s * j->inv_s;
-    struct Src { int idx; int64_t rows, n, npad; double scale; };
-    const Src src[SP_N] = {{DST_T2A, v * v * o, o, op, sT}, {DST_T2B, v * o * o, v, vp, sT},
-                           {DST_WD1, v * o * o, o, op, sI}, {DST_VD2, vd2_elems / std::max<int64_t>(v, 1), v, vp, sI}};
-    for (int k = 0; k < SP_N && !rc; ++k) {
-        const size_t n = (size_t)(src[k].rows * src[k].npad);
+    // Box tables: global box ids per space, first index and valid rows.
+    std::vector<int32_t> tile_box(nt), vrow0, vn, orow0, on;
+    for (int64_t b = 1; b <= nt; ++b) {
+        const bool virt = b > noab;
+        const int bx = virt ? SX_BV : SX_BO;
+        std::vector<int32_t> &row0 = virt ? vrow0 : orow0, &nvalid = virt ? vn : on;
+        tile_box[b - 1] = (int32_t)row0.size();
+        for (int64_t s0 = 0; s0 < t.r(b); s0 += bx) {
+            row0.push_back((int32_t)(t.start(b) + s0));
+            nvalid.push_back((int32_t)std::min<int64_t>(bx, t.r(b) - s0));
+        }
+    }
+    const int64_t NOB = (int64_t)orow0.size(), NVB = (int64_t)vrow0.size();
+    j->nob = (int32_t)NOB;
+    j->nvb = (int32_t)NVB;
+    // Vd2 tile pairs (B <= C): first block, FP64 region offset, dims.
+    std::vector<int64_t> pblk0, poff, pair_blk(nvab * nvab, -1);
+    std::vector<int32_t> pdim;
+    int64_t nvd2 = 0;
+    for (int64_t B = noab + 1; B <= nt; ++B)
+        for (int64_t C = B; C <= nt; ++C) {
+            const int64_t off = j->pair_host[(B - noab - 1) * nvab + (C - noab - 1)];
+            if (off < 0) continue;
+            const int64_t nbB = (t.r(B) + SX_BV - 1) / SX_BV, nbC = (t.r(C) + SX_BV - 1) / SX_BV;
+            pair_blk[(B - noab - 1) * nvab + (C - noab - 1)] = nvd2;
+            pblk0.push_back(nvd2);
+            poff.push_back(off);
+            pdim.push_back((int32_t)t.r(B));
+            pdim.push_back((int32_t)t.r(C));
+            pdim.push_back((int32_t)nbC);
+            nvd2 += nbB * nbC * NOB * nkv;
+        }
+    const int npairs = (int)poff.size();
+    pblk0.push_back(nvd2);
+    // Tables on the device (one buffer, 8-byte aligned parts).
+    std::vector<int64_t> tab;
+    auto put32 = [&](const std::vector<int32_t> &x) {
+        const size_t at = tab.size();
+        tab.resize(at + (x.size() + 1) / 2, 0);
+        if (!x.empty()) std::memcpy(tab.data() + at, x.data(), x.size() * sizeof(int32_t));
+        return at;
+    };
+    auto put64 = [&](const std::vector<int64_t> &x) {
+        const size_t at = tab.size();
+        tab.insert(tab.end(), x.begin(), x.end());
+        return at;
+    };
+    const size_t o_vrow0 = put32(vrow0), o_vn = put32(vn), o_orow0 = put32(orow0), o_on = put32(on);
+    const size_t o_pblk0 = put64(pblk0), o_poff = put64(poff), o_pdim = put32(pdim);
+    const size_t o_tbox = put32(tile_box), o_pairblk = put64(pair_blk);
+    int64_t *tab_d = (int64_t *)gpu_get(std::max<size_t>(tab.size(), 1) * sizeof(int64_t));
+    j->err_d = (int *)gpu_get(sizeof(int));
+    j->err_h = (int *)host_get(sizeof(int));
+    if (!tab_d || !j->err_d || !j->err_h) {
+        gpu_put(tab_d);
+        mixed_release(j);
+        return fail(SDT_ERR_NOMEM, "mixed form: tables");
+    }
+    j->tile_box_d = tab_d;  // owns the whole table buffer
+    rc = cuda_check(cudaMemcpyAsync(tab_d, tab.data(), tab.size() * sizeof(int64_t), cudaMemcpyHostToDevice, st),
+                    "mixed form: tables");
+    j->tile_box_off = (int64_t)o_tbox;
+    j->pair_blk_off = (int64_t)o_pairblk;
+    // Block-major split operands.
+    const int64_t nblk[L_N] = {NVB * NOB * NOB * nko, NVB * NOB * NOB * nkv, NVB * NVB * NOB * nko, nvd2};
+    const int srcidx[L_N] = {DST_WD1, DST_T2B, DST_T2A, DST_VD2};
+    const double scale[L_N] = {sI, sT, sT, sI};
+    for (int l = 0; l < L_N && !rc; ++l) {
+        const int rows = l < L_T2A ? 128 : 256;
+        const size_t bytes = (size_t)nblk[l] * rows * 32;
         for (int h = 0; h < 2; ++h) {
-            j->sp[2 * k + h] = gpu_get(std::max<size_t>(n, 1) * es);
-            if (!j->sp[2 * k + h]) {
+            j->sp[2 * l + h] = gpu_get(std::max<size_t>(bytes, 16));
+            if (!j->sp[2 * l + h]) {
                 mixed_release(j);
                 return fail(SDT_ERR_NOMEM, "mixed form: split operand allocation");
             }
-            j->sp_n[2 * k + h] = n;
+            j->sp_n[2 * l + h] = bytes;
         }
-        void *hi = j->sp[2 * k], *lo = j->sp[2 * k + 1];
-        const double *s = j->arr[src[k].idx];
-        const unsigned gb = grid_for((int64_t)n);
-        if (type == TM_F32)
-            split_rows_kernel<TM_F32><<<gb, 256, 0, st>>>(s, hi, lo, src[k].rows, src[k].n, src[k].npad, src[k].scale);
-        else if (type == TM_BF16)
-            split_rows_kernel<TM_BF16><<<gb, 256, 0, st>>>(s, hi, lo, src[k].rows, src[k].n, src[k].npad, src[k].scale);
-        else
-            split_rows_kernel<TM_F16><<<gb, 256, 0, st>>>(s, hi, lo, src[k].rows, src[k].n, src[k].npad, src[k].scale);
+        if (nblk[l] == 0) continue;
+        PackArgs g;
+        g.src = j->arr[srcidx[l]];
+        g.hi = (uint8_t *)j->sp[2 * l];
+        g.lo = (uint8_t *)j->sp[2 * l + 1];
+        g.nblocks = nblk[l];
+        g.layout = l;
+        g.nk = (l == L_WD1 || l == L_T2A) ? (int)nko : (int)nkv;
+        g.ke = ke;
+        g.es = es;
+        g.o = o;
+        g.v = v;
+        g.nob = (int)NOB;
+        g.nvb = (int)NVB;
+        const int32_t *t32 = (const int32_t *)tab_d;
+        g.vrow0 = t32 + 2 * o_vrow0;
+        g.vn = t32 + 2 * o_vn;
+        g.orow0 = t32 + 2 * o_orow0;
+        g.on = t32 + 2 * o_on;
+        g.pblk0 = tab_d + o_pblk0;
+        g.poff = tab_d + o_poff;
+        g.pdim = t32 + 2 * o_pdim;
+        g.npairs = npairs;
+        g.scale = scale[l];
+        const unsigned gb = grid_for(nblk[l] * rows * ke);
+        if (type == TM_F32) pack_blocks_kernel<TM_F32><<<gb, 256, 0, st>>>(g);
+        else if (type == TM_BF16) pack_blocks_kernel<TM_BF16><<<gb, 256, 0, st>>>(g);
+        else pack_blocks_kernel<TM_F16><<<gb, 256, 0, st>>>(g);
         count_launch();
     }
     // FP32 copies of T1 [v][o] and the vvoo block [v][v][o][o] for the s1 terms.
     const int64_t n_t1 = v * o, n_u = (int64_t)j->arr_n[DST_UD];
-    j->t1f = (float *)gpu_get(std::max<int64_t>(n_t1, 1) * sizeof(float));
-    j->uf = (float *)gpu_get(std::max<int64_t>(n_u, 1) * sizeof(float));
-    if (!j->t1f || !j->uf) {
-        mixed_release(j);
-        return fail(SDT_ERR_NOMEM, "mixed form: FP32 copies");
-    }
-    to_f32_kernel<<<grid_for(n_t1), 256, 0, st>>>(j->arr[DST_T1], j->t1f, n_t1);
-    count_launch();
-    to_f32_kernel<<<grid_for(n_u), 256, 0, st>>>(j->arr[DST_UD], j->uf, n_u);
-    count_launch();
-    if (!rc) rc = cuda_check(cudaGetLastError(), "mixed form: split");
-    if (rc) {
-        mixed_release(j);
-        return rc;
-    }
-    // Tensor maps (32-byte swizzle, 32-byte K rows).
-    const uint64_t E = (uint64_t)es;
-    const uint32_t KE = (uint32_t)ke;
-    {
-        const uint64_t d[4] = {(uint64_t)vp, (uint64_t)o, (uint64_t)o, (uint64_t)v};
-        const uint64_t sb[3] = {vp * E, o * vp * E, o * o * vp * E};
-        const uint32_t box[4] = {KE, 4, 4, 8};
-        rc = make_tmap(&j->maps[0], j->sp[2 * SP_T2B], type, 4, d, sb, box, 32);
-        if (!rc) rc = make_tmap(&j->maps[1], j->sp[2 * SP_T2B + 1], type, 4, d, sb, box, 32);
-    }
     if (!rc) {
-        const uint64_t d[4] = {(uint64_t)op, (uint64_t)o, (uint64_t)v, (uint64_t)v};
-        const uint64_t sb[3] = {op * E, o * op * E, v * o * op * E};
-        const uint32_t box[4] = {KE, 4, 8, 8};
-        rc = make_tmap(&j->maps[2], j->sp[2 * SP_T2A], type, 4, d, sb, box, 32);
-        if (!rc) rc = make_tmap(&j->maps[3], j->sp[2 * SP_T2A + 1], type, 4, d, sb, box, 32);
-    }
-    if (!rc) {
-        const uint64_t d[4] = {(uint64_t)op, (uint64_t)o, (uint64_t)o, (uint64_t)v};
-        const uint64_t sb[3] = {op * E, o * op * E, o * o * op * E};
-        const uint32_t box[4] = {KE, 4, 4, 8};
-        rc = make_tmap(&j->maps[4], j->sp[2 * SP_WD1], type, 4, d, sb, box, 32);
-        if (!rc) rc = make_tmap(&j->maps[5], j->sp[2 * SP_WD1 + 1], type, 4, d, sb, box, 32);
-    }
-    std::vector<CUtensorMap> vmaps;
-    std::vector<int32_t> pid(nvab * nvab, -1);
-    for (int64_t B = noab + 1; B <= noab + nvab && !rc; ++B)
-        for (int64_t C = B; C <= noab + nvab && !rc; ++C) {
-            const int64_t off = j->pair_host[(B - noab - 1) * nvab + (C - noab - 1)];
-            if (off < 0) continue;
-            const int64_t nB = t.r(B), nC = t.r(C);
-            const int64_t soff = off / v * vp;  // elements; a multiple of 16 bytes
-            const uint64_t d[4] = {(uint64_t)vp, (uint64_t)o, (uint64_t)nC, (uint64_t)nB};
-            const uint64_t sb[3] = {vp * E, o * vp * E, nC * o * vp * E};
-            const uint32_t box[4] = {KE, 4, 8, 8};
-            CUtensorMap mh, ml;
-            rc = make_tmap(&mh, (const uint8_t *)j->sp[2 * SP_VD2] + soff * es, type, 4, d, sb, box, 32);
-            if (!rc) rc = make_tmap(&ml, (const uint8_t *)j->sp[2 * SP_VD2 + 1] + soff * es, type, 4, d, sb, box, 32);
-            pid[(B - noab - 1) * nvab + (C - noab - 1)] = (int32_t)(vmaps.size() / 2);
-            vmaps.push_back(mh);
-            vmaps.push_back(ml);
+        j->t1f = (float *)gpu_get(std::max<int64_t>(n_t1, 1) * sizeof(float));
+        j->uf = (float *)gpu_get(std::max<int64_t>(n_u, 1) * sizeof(float));
+        if (!j->t1f || !j->uf) {
+            mixed_release(j);
+            return fail(SDT_ERR_NOMEM, "mixed form: FP32 copies");
         }
-    if (rc) {
-        mixed_release(j);
-        return rc;
+        to_f32_kernel<<<grid_for(n_t1), 256, 0, st>>>(j->arr[DST_T1], j->t1f, n_t1);
+        count_launch();
+        to_f32_kernel<<<grid_for(n_u), 256, 0, st>>>(j->arr[DST_UD], j->uf, n_u);
+        count_launch();
+        rc = cuda_check(cudaGetLastError(), "mixed form: split");
     }
-    j->vd2_maps = (CUtensorMap *)gpu_get(std::max<size_t>(vmaps.size(), 1) * sizeof(CUtensorMap));
-    j->pair_id = (int32_t *)gpu_get(std::max<size_t>(pid.size(), 1) * sizeof(int32_t));
-    j->err_d = (int *)gpu_get(sizeof(int));
-    j->err_h = (int *)host_get(sizeof(int));
-    if (!j->vd2_maps || !j->pair_id || !j->err_d || !j->err_h) {
-        mixed_release(j);
-        return fail(SDT_ERR_NOMEM, "mixed form: tables");
-    }
-    if (!vmaps.empty())
-        rc = cuda_check(cudaMemcpyAsync(j->vd2_maps, vmaps.data(), vmaps.size() * sizeof(CUtensorMap),
-                                        cudaMemcpyHostToDevice, st), "mixed form: maps");
-    if (!rc && !pid.empty())
-        rc = cuda_check(cudaMemcpyAsync(j->pair_id, pid.data(), pid.size() * sizeof(int32_t), cudaMemcpyHostToDevice,
-                                        st), "mixed form: maps");
     if (!rc) rc = cuda_check(cudaStreamSynchronize(st), "mixed form: prepare");
     if (rc) {
         mixed_release(j);
@@ -782,16 +989,14 @@ int mixed_prepare(sdt_job *j, int type, cudaStream_t st) {
     return SDT_OK;
 }
 
-int mixed_launch(sdt_job *j, int64_t items, int64_t n, cudaStream_t st) {
+int mixed_launch(sdt_job *j, int64_t n_super, int64_t n, cudaStream_t st) {
     const Tiling &t = j->t;
     const int type = j->mixed_type;
     const int ke = type == TM_F32 ? 8 : 16;
     SplitParams p;
-    p.t2b_hi = j->maps[0]; p.t2b_lo = j->maps[1];
-    p.t2a_hi = j->maps[2]; p.t2a_lo = j->maps[3];
-    p.wd1_hi = j->maps[4]; p.wd1_lo = j->maps[5];
-    p.vd2_maps = j->vd2_maps;
-    p.pair_id = j->pair_id;
+    for (int k = 0; k < 2 * L_N; ++k) p.blk[k] = (const uint8_t *)j->sp[k];
+    p.tile_box = (const int32_t *)(j->tile_box_d + j->tile_box_off);
+    p.pair_blk = j->tile_box_d + j->pair_blk_off;
     p.T1f = j->t1f;
     p.Uf = j->uf;
     p.evl = j->evl_d;
@@ -802,33 +1007,63 @@ int mixed_launch(sdt_job *j, int64_t items, int64_t n, cudaStream_t st) {
     p.nvir = t.nvir;
     p.nk_o = (int32_t)((t.nocc + ke - 1) / ke);
     p.nk_v = (int32_t)((t.nvir + ke - 1) / ke);
+    p.nob = j->nob;
+    p.nvb = j->nvb;
     p.kseg = j->mixed_kseg;
     p.klist = j->klist_d;
     p.item_pref = j->pref_d;
+    p.super_pref = j->spref_d;
     p.factor = j->factor_d;
     p.n_tasks = n;
-    p.items = items;
+    p.n_super = n_super;
     p.inv_s = j->inv_s;
     p.inv_s2 = j->inv_s2;
     p.part = j->part_d;
     p.err = j->err_d;
-    int nsm = 0;
-    int rc = cuda_check(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, j->dev), "mixed form");
-    if (rc) return rc;
-    const unsigned grid = (unsigned)std::max<int64_t>(1, std::min<int64_t>(items, nsm));
+    const bool cluster = j->mixed_cluster == 4;
     auto launch = [&](auto kern) {
         int r = cuda_check(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, SX_SMEM_ALLOC),
                            "mixed form: smem attribute");
         if (r) return r;
-        kern<<<grid, SX_THREADS, SX_SMEM_ALLOC, st>>>(p);
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeClusterDimension;
+        attr[0].val.clusterDim.x = 4;
+        attr[0].val.clusterDim.y = 1;
+        attr[0].val.clusterDim.z = 1;
+        cudaLaunchConfig_t cfg = {};
+        cfg.blockDim = dim3(SX_THREADS);
+        cfg.dynamicSmemBytes = SX_SMEM_ALLOC;
+        cfg.stream = st;
+        if (cluster) {
+            cfg.attrs = attr;
+            cfg.numAttrs = 1;
+            cfg.gridDim = dim3(4);
+            int ncl = 0;
+            r = cuda_check(cudaOccupancyMaxActiveClusters(&ncl, kern, &cfg), "mixed form: cluster occupancy");
+            if (r) return r;
+            if (ncl < 1) return fail(SDT_ERR_CUDA, "mixed form: no cluster of 4 CTAs fits on this device");
+            cfg.gridDim = dim3((unsigned)(4 * std::max<int64_t>(1, std::min<int64_t>(ncl, n_super))));
+        } else {
+            int nsm = 0;
+            r = cuda_check(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, j->dev), "mixed form");
+            if (r) return r;
+            cfg.gridDim = dim3((unsigned)std::max<int64_t>(1, std::min<int64_t>(nsm, n_super)));
+        }
+        r = cuda_check(cudaLaunchKernelEx(&cfg, kern, p), "mixed form: fused kernel");
         count_launch();
-        return cuda_check(cudaGetLastError(), "mixed form: fused kernel");
+        return r;
     };
-    rc = cuda_check(cudaMemsetAsync(j->err_d, 0, sizeof(int), st), "mixed form");
+    int rc = cuda_check(cudaMemsetAsync(j->err_d, 0, sizeof(int), st), "mixed form");
     if (rc) return rc;
-    if (type == TM_F32) rc = launch(split_fused_kernel<TM_F32>);
-    else if (type == TM_BF16) rc = launch(split_fused_kernel<TM_BF16>);
-    else rc = launch(split_fused_kernel<TM_F16>);
+    if (cluster) {
+        if (type == TM_F32) rc = launch(split_fused_kernel<TM_F32, 4>);
+        else if (type == TM_BF16) rc = launch(split_fused_kernel<TM_BF16, 4>);
+        else rc = launch(split_fused_kernel<TM_F16, 4>);
+    } else {
+        if (type == TM_F32) rc = launch(split_fused_kernel<TM_F32, 1>);
+        else if (type == TM_BF16) rc = launch(split_fused_kernel<TM_BF16, 1>);
+        else rc = launch(split_fused_kernel<TM_F16, 1>);
+    }
     if (!rc) rc = cuda_check(cudaMemcpyAsync(j->err_h, j->err_d, sizeof(int), cudaMemcpyDeviceToHost, st),
                              "mixed form");
     return rc;

@@ -136,6 +136,10 @@ class TriplesJob:
         (8 TF32 or 16 BF16/FP16 values each; 0: once per contraction term)."""
         _capi.check(self._lib.sdt_job_set_mixed_segment(self._h, int(chunks)), "sdt_job_set_mixed_segment")
 
+    def set_mixed_cluster(self, ctas: int) -> None:
+        """Mixed form: clusters of 1 (default) or 4 CTAs sharing operand tiles."""
+        _capi.check(self._lib.sdt_job_set_mixed_cluster(self._h, int(ctas)), "sdt_job_set_mixed_cluster")
+
     @property
     def last_kernel_ms(self) -> float:
         return float(self._lib.sdt_job_last_kernel_ms(self._h))

@@ -157,3 +157,22 @@ def test_mixed_persistent_many_items(cuda_device):
             m = job.run(kl, precision=PREC[form])
             b = MIXED_BOUND[form]
             assert m[0] == pytest.approx(f[0], rel=b) and m[1] == pytest.approx(f[1], rel=b)
+
+
+@pytest.mark.parametrize("form", ["fp16", "tf32"])
+def test_mixed_cluster_of_four(cuda_device, form):
+    """Clusters of 4 CTAs (multicast operand tiles, (j,k) box pairs, odd box
+    counts leave idle CTAs) give the same bits as single CTAs."""
+    import nwchem_gb300 as ng
+    t = ng.Tiling([3, 5, 6], [9, 6, 10, 17]).with_evl(8)
+    files = ng.synth_inputs(t, 8)
+    kl = ng.task_list(t)
+    with ng.TriplesJob(t) as job:
+        job.load(*files)
+        f = job.run(kl)
+        a = job.run(kl, per_task=True, precision=PREC[form])
+        job.set_mixed_cluster(4)
+        b = job.run(kl, per_task=True, precision=PREC[form])
+    assert a[0] == b[0] and a[1] == b[1] and np.array_equal(a[2], b[2])
+    bnd = MIXED_BOUND[form]
+    assert b[0] == pytest.approx(f[0], rel=bnd) and b[1] == pytest.approx(f[1], rel=bnd)
