@@ -404,6 +404,65 @@ def workload_o64v512(args) -> None:
     print(json.dumps(out), flush=True)
 
 
+def workload_sym8(args) -> None:
+    """Blocked spatial symmetry (8 irreps; o=148 as 8 tiles of 8-32, v=336 as
+    12 tiles of 16-64, seed 3): the first 4096 tuples of the weight order in
+    one plan -- the autotuner's split form and per-size-class work-unit
+    shapes, one persistent launch per shape drawing from a device queue,
+    captured as a CUDA graph and replayed; the FP64 form on a seeded sample
+    of 16 tuples for the error."""
+    import torch
+
+    import nwchem_gb300 as ng
+    from nwchem_gb300 import autotune
+    torch.cuda.set_device(0)
+    t = ng.config_tiling(3)
+    kl = ng.task_list(t)[:4096]
+    t0 = time.perf_counter()
+    files = ng.synth_inputs(t, 3)
+    gen_s = time.perf_counter() - t0
+    samp = np.sort(np.random.default_rng(0).choice(len(kl), 16, replace=False))
+    stream = torch.cuda.Stream()
+    fl_all, fl_s = ng.flops(t, kl), ng.flops(t, kl[samp])
+    out = {"workload": f"{t.name}: 8 irreps, occupied tiles {t.occ}, virtual tiles {t.vir}, seed 3, "
+                       f"first 4096 of {len(ng.task_list(t))} tuples", "flops": fl_all}
+    with ng.TriplesJob(t) as job:
+        t0 = time.perf_counter()
+        job.load(*files, stream=stream)
+        stream.synchronize()
+        out["load_s"] = time.perf_counter() - t0
+        job.set_timing(True)
+        f = job.run(kl[samp], stream=stream, per_task=True)
+        out["fp64_sample"] = {"tuples": 16, "tflops": fl_s / job.last_kernel_ms / 1e9, "E": list(f[:2])}
+        t0 = time.perf_counter()
+        tuner = autotune.Autotuner(job, forms=("fp16", "tf32"), sample=4)
+        plan, d = tuner.plan(kl, capture=True, stream=stream)
+        out["autotune"] = {"s": time.perf_counter() - t0, "form": d["form"], "shapes": d["shapes"],
+                           "classes": len(d["shapes"])}
+        with plan:
+            plan.run(stream=stream)                      # warm-up replay
+            ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            ev0.record(stream)
+            reps = max(1, min(args.steps, 3))
+            for _ in range(reps):
+                e = plan.run(stream=stream)
+            ev1.record(stream)
+            stream.synchronize()
+            g_s = ev0.elapsed_time(ev1) / 1e3 / reps
+            out["mixed_graph"] = {"form": d["form"], "tflops": fl_all / g_s / 1e12, "s_per_run": g_s, "E": list(e),
+                                  "items": plan.items}
+        prec = autotune.FORMS[d["form"]]
+        m = job.run(kl[samp], stream=stream, per_task=True, precision=prec)
+        out["mixed_sample_rel_err"] = [(m[0] - f[0]) / abs(f[0]), (m[1] - f[1]) / abs(f[1]),
+                                       ((m[1] - m[0]) - (f[1] - f[0])) / abs(f[1] - f[0])]
+        t0 = time.perf_counter()
+        job.run(kl, stream=stream, precision=prec)       # one-shot path (plan built and freed per call)
+        out["mixed_one_shot_s"] = time.perf_counter() - t0
+        out["device_bytes"] = job.device_bytes
+    out["input_generation_s"] = gen_s
+    print(json.dumps(out), flush=True)
+
+
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -413,7 +472,7 @@ def main() -> None:
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--profile", action="store_true", help="small single-launch case for ncu")
     ap.add_argument("--tuples", type=int, default=2, help="tuples in the --profile case")
-    ap.add_argument("--workload", default="o40v300", choices=["o40v300", "o64v512"])
+    ap.add_argument("--workload", default="o40v300", choices=["o40v300", "o64v512", "sym8"])
     ap.add_argument("--case", default="o40v114", choices=["o40v114", "o64v128"], help="--profile case")
     ap.add_argument("--kseg", type=int, default=0, help="mixed form: K chunks per accumulator drain")
     ap.add_argument("--mixed", default="", choices=["", "tf32", "bf16", "fp16"],
@@ -425,6 +484,8 @@ def main() -> None:
     b.build()
     if args.workload == "o64v512":
         workload_o64v512(args)
+    elif args.workload == "sym8":
+        workload_sym8(args)
     elif args.profile:
         profile_case(args)
     elif args.impl == "reference":

@@ -237,6 +237,30 @@ int sdt_job_set_mixed_cluster(sdt_job *job, int ctas);
 int sdt_job_set_timing(sdt_job *job, int on);
 double sdt_job_last_kernel_ms(const sdt_job *job);
 
+/* Plans (no reference counterpart): a prepared evaluation of a tuple
+ * list.  sdt_plan_create checks the list, builds the work indexes, sizes
+ * the persistent launches (and, for a mixed precision, encodes the job's
+ * split operands if needed) and uploads them; ctas (optional, one per
+ * tuple, 1 or 4) picks the mixed kernel's work-unit shape per tuple (4: a
+ * cluster of 4 CTAs takes a 2x2 tile of (j,k) sub-boxes).
+ * sdt_plan_launch only enqueues device work -- per group a queue reset and
+ * one persistent kernel, the compensated sums and the copy of the results
+ * to pinned host memory -- and can be recorded by stream capture;
+ * sdt_plan_capture records one launch into a CUDA graph, which
+ * sdt_plan_run then replays (else it launches), synchronises the stream and
+ * returns E[T], E(T) and, optionally, the per-tuple pairs in the caller's
+ * order.  A plan is bound to its job; destroy it after its last run. */
+typedef struct sdt_plan sdt_plan;
+int sdt_plan_create(sdt_job *job, const int64_t *klist, int64_t n,
+                    int precision, const int32_t *ctas, sdt_plan **plan);
+int sdt_plan_launch(sdt_plan *plan, void *stream);
+int sdt_plan_capture(sdt_plan *plan, void *stream);
+int sdt_plan_run(sdt_plan *plan, void *stream, double *energy,
+                 double *per_task);
+int sdt_plan_destroy(sdt_plan *plan);
+/* Sub-box work items of a plan. */
+int64_t sdt_plan_items(const sdt_plan *plan);
+
 /* One-shot replacement for ccsd_t(d_t1,k_t1_offset,d_t2,k_t2_offset,
  * d_v2,k_v2_offset,energy1,energy2,size_t1) (ccsd_t.F:19-20): builds the
  * tuple list, loads the files, runs every tuple and returns E[T] in

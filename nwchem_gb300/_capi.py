@@ -60,6 +60,13 @@ def _declare(lib):
         "sdt_job_set_mixed_cluster": (C.c_int, [C.c_void_p, C.c_int]),
         "sdt_job_last_kernel_ms": (C.c_double, [C.c_void_p]),
         "sdt_probe_fp64_tflops": (C.c_double, [C.c_int]),
+        "sdt_plan_create": (C.c_int, [C.c_void_p, PI64, C.c_int64, C.c_int, C.POINTER(C.c_int32),
+                                      C.POINTER(C.c_void_p)]),
+        "sdt_plan_launch": (C.c_int, [C.c_void_p, C.c_void_p]),
+        "sdt_plan_capture": (C.c_int, [C.c_void_p, C.c_void_p]),
+        "sdt_plan_run": (C.c_int, [C.c_void_p, C.c_void_p, PD, PD]),
+        "sdt_plan_destroy": (C.c_int, [C.c_void_p]),
+        "sdt_plan_items": (C.c_int64, [C.c_void_p]),
         "sdt_tc_selftest": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]),
         "sdt_tc_selftest16": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int,
                                         C.c_void_p]),

@@ -108,8 +108,9 @@ struct FusedParams {
     const int64_t *klist;     // [n][7]
     const int64_t *item_pref; // [n+1]
     const double *factor;     // [n]
-    int64_t n_tasks, item_base;
+    int64_t n_tasks, n_items;
     double *part;             // [items][2]
+    unsigned long long *queue;  // work-item counter, zero at launch
 };
 
 struct TupleCtx {
@@ -240,12 +241,22 @@ __device__ __forceinline__ void run_term(const FusedParams &p, const TupleCtx &t
     __syncthreads();
 }
 
+// Persistent: each CTA draws sub-boxes from the device queue until it is
+// empty.  A sub-box's pair depends only on its index, not on the CTA.
 __global__ void __launch_bounds__(kThreads, 4) fused_fp64_kernel(const FusedParams p) {
     __shared__ double X[NX];
     __shared__ int32_t st[kMaxTiles][4];
     __shared__ double red[2][kThreads / 32];
+    __shared__ long long s_item;
 
-    const int64_t item = p.item_base + blockIdx.x;
+    const int ntiles = p.noab + p.nvab;
+    for (int e = threadIdx.x; e < ntiles * 4; e += kThreads) st[e >> 2][e & 3] = p.tiles[e];
+    for (;;) {
+    if (threadIdx.x == 0) s_item = (long long)atomicAdd(p.queue, 1ull);
+    for (int e = threadIdx.x; e < NX; e += kThreads) X[e] = 0.0;
+    __syncthreads();
+    const int64_t item = s_item;
+    if (item >= p.n_items) break;
     // Tuple owning this item: last q with item_pref[q] <= item.
     int64_t lo = 0, hi = p.n_tasks - 1;
     while (lo < hi) {
@@ -255,11 +266,6 @@ __global__ void __launch_bounds__(kThreads, 4) fused_fp64_kernel(const FusedPara
     }
     const int64_t tq = lo;
     int64_t local = item - p.item_pref[tq];
-
-    const int ntiles = p.noab + p.nvab;
-    for (int e = threadIdx.x; e < ntiles * 4; e += kThreads) st[e >> 2][e & 3] = p.tiles[e];
-    for (int e = threadIdx.x; e < NX; e += kThreads) X[e] = 0.0;
-    __syncthreads();
 
     TupleCtx t;
 #pragma unroll
@@ -332,6 +338,8 @@ __global__ void __launch_bounds__(kThreads, 4) fused_fp64_kernel(const FusedPara
         p.part[2 * item] = x;
         p.part[2 * item + 1] = y;
     }
+    __syncthreads();  // red, X and s_item are reused by the next item
+    }
 }
 
 // Per-tuple sums of item partials (fixed order, compensated).
@@ -366,13 +374,45 @@ __global__ void __launch_bounds__(256) tuple_sum_kernel(const double *__restrict
 
 }  // namespace
 
-int finish_run(sdt_job *j, int64_t n, cudaStream_t st) {
+int tuple_sums(const double *part, const int64_t *gpref, int64_t n, double *task, double *out, cudaStream_t st) {
     for (int64_t q0 = 0; q0 < n; q0 += 65535) {
         const unsigned nb = (unsigned)std::min<int64_t>(65535, n - q0);
-        tuple_sum_kernel<<<nb, 256, 0, st>>>(j->part_d, j->pref_d + q0, nb, j->task_d + 2 * q0);
+        tuple_sum_kernel<<<nb, 256, 0, st>>>(part, gpref + q0, nb, task + 2 * q0);
         count_launch();
     }
-    return reduce_pairs(j->task_d, n, j->out_d, st);
+    return reduce_pairs(task, n, out, st);
+}
+
+int fp64_grid(sdt_job *j, int64_t items, int *grid) {
+    int nsm = 0, per_sm = 0;
+    int rc = cuda_check(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, j->dev), "FP64 form");
+    if (!rc) rc = cuda_check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fused_fp64_kernel, kThreads, 0),
+                             "FP64 form");
+    if (rc) return rc;
+    *grid = (int)std::max<int64_t>(1, std::min<int64_t>(items, (int64_t)nsm * std::max(per_sm, 1)));
+    return SDT_OK;
+}
+
+int fp64_launch(sdt_job *j, const LaunchArgs &a, cudaStream_t st) {
+    const Tiling &t = j->t;
+    FusedParams p;
+    p.T1d = j->arr[DST_T1]; p.T2a = j->arr[DST_T2A]; p.T2b = j->arr[DST_T2B];
+    p.Vd2 = j->arr[DST_VD2]; p.Wd1 = j->arr[DST_WD1]; p.Ud = j->arr[DST_UD];
+    p.pair_off = j->pair_off;
+    p.evl = j->evl_d;
+    p.tiles = j->tiles;
+    p.noab = (int32_t)t.noab; p.nvab = (int32_t)t.nvab;
+    p.nocc = t.nocc; p.nvir = t.nvir;
+    p.klist = a.klist; p.item_pref = a.item_pref; p.factor = a.factor;
+    p.n_tasks = a.n;
+    p.n_items = a.items;
+    p.part = a.part;
+    p.queue = a.queue;
+    int rc = cuda_check(cudaMemsetAsync(a.queue, 0, sizeof(unsigned long long), st), "FP64 form");
+    if (rc) return rc;
+    fused_fp64_kernel<<<(unsigned)a.grid, kThreads, 0, st>>>(p);
+    count_launch();
+    return cuda_check(cudaGetLastError(), "FP64 form: fused kernel");
 }
 
 }  // namespace sdt
@@ -656,8 +696,8 @@ extern "C" int sdt_job_load(sdt_job *j, const sdt_file *f1, const sdt_file *f2,
     return SDT_OK;
 }
 
-namespace {
 // Multiplicity factor of a tuple (ccsd_t_dot.F:52-66).
+namespace sdt {
 double tuple_factor(const int64_t *k, bool restricted) {
     double f = restricted ? 2.0 : 1.0;
     if (k[0] == k[1] && k[1] == k[2]) f /= 6.0;
@@ -666,147 +706,7 @@ double tuple_factor(const int64_t *k, bool restricted) {
     else if (k[3] == k[4] || k[4] == k[5]) f /= 2.0;
     return f;
 }
-
-bool grow(void **p, size_t *cap, size_t bytes) {
-    if (*cap >= bytes && *p) return true;
-    gpu_put(*p);
-    *p = gpu_get(bytes);
-    *cap = *p ? bytes : 0;
-    return *p != nullptr;
-}
-}  // namespace
-
-extern "C" int sdt_job_run(sdt_job *j, const int64_t *klist, int64_t n, int precision,
-                           double *energy, double *per_task, void *stream) {
-    if (!j || !energy || (n > 0 && !klist)) return fail(SDT_ERR_ARG, "sdt_job_run: null argument");
-    if (!j->loaded) return fail(SDT_ERR_STATE, "sdt_job_run: sdt_job_load has not succeeded");
-    if (precision < SDT_PREC_FP64 || precision > SDT_PREC_MIXED_FP16)
-        return fail(SDT_ERR_ARG, "sdt_job_run: unknown precision");
-    const bool mixed = precision != SDT_PREC_FP64;
-    const int mtype = precision == SDT_PREC_MIXED_TF32 ? TM_F32 : precision == SDT_PREC_MIXED_BF16 ? TM_BF16 : TM_F16;
-    // Sub-box edges: 4 in every index (FP64); 8 virtual x 4 occupied (mixed).
-    const int box_v = mixed ? 8 : BOX, box_o = BOX;
-    energy[0] = energy[1] = 0.0;
-    if (n == 0) return SDT_OK;
-    cudaStream_t st = stream ? (cudaStream_t)stream : lib_stream();
-    const Tiling &t = j->t;
-    const int64_t nt = t.noab + t.nvab;
-    std::vector<int64_t> pref(n + 1, 0), spref(n + 1, 0);
-    std::vector<double> fac(n);
-    for (int64_t q = 0; q < n; ++q) {
-        const int64_t *k = klist + 7 * q;
-        int64_t boxes = 1, supers = 1;  // mixed form: clusters of 4 take (j,k) box pairs
-        for (int d = 0; d < 6; ++d) {
-            const bool virt = d < 3;
-            if (k[d] < 1 || k[d] > nt || (virt ? k[d] <= t.noab : k[d] > t.noab))
-                return fail(SDT_ERR_ARG, "sdt_job_run: tuple tile out of range");
-            const int bx = virt ? box_v : box_o;
-            const int64_t nb = (t.r(k[d]) + bx - 1) / bx;
-            boxes *= nb;
-            supers *= (d >= 4 && j->mixed_cluster == 4) ? (nb + 1) / 2 : nb;
-        }
-        spref[q + 1] = spref[q] + supers;
-        if (!(k[0] <= k[1] && k[1] <= k[2] && k[3] <= k[4] && k[4] <= k[5]))
-            return fail(SDT_ERR_ARG, "sdt_job_run: tuple tiles not sorted");
-        pref[q + 1] = pref[q] + boxes;
-        fac[q] = tuple_factor(k, t.restricted != 0);
-    }
-    const int64_t items = pref[n];
-    void *p0 = j->klist_d, *p1 = j->pref_d, *p2 = j->factor_d, *p3 = j->task_d, *p4 = j->part_d, *p5 = j->spref_d;
-    size_t c_tasks = j->cap_tasks, c_items = j->cap_items;
-    // Workspace sized by the largest request so far.
-    if (c_tasks < (size_t)n || !p0) {
-        size_t cap = 0;
-        bool ok = grow(&p0, &cap, 7 * n * sizeof(int64_t));
-        cap = 0; ok = ok && grow(&p1, &cap, (n + 1) * sizeof(int64_t));
-        cap = 0; ok = ok && grow(&p2, &cap, n * sizeof(double));
-        cap = 0; ok = ok && grow(&p3, &cap, 2 * n * sizeof(double));
-        cap = 0; ok = ok && grow(&p5, &cap, (n + 1) * sizeof(int64_t));
-        if (!ok) return fail(SDT_ERR_NOMEM, "sdt_job_run: workspace");
-        c_tasks = n;
-    }
-    if (c_items < (size_t)items || !p4) {
-        size_t cap = 0;
-        if (!grow(&p4, &cap, 2 * items * sizeof(double))) return fail(SDT_ERR_NOMEM, "sdt_job_run: partials");
-        c_items = items;
-    }
-    j->klist_d = (int64_t *)p0; j->pref_d = (int64_t *)p1; j->factor_d = (double *)p2;
-    j->task_d = (double *)p3; j->part_d = (double *)p4; j->spref_d = (int64_t *)p5;
-    j->cap_tasks = c_tasks; j->cap_items = c_items;
-    if (!j->out_d) j->out_d = (double *)gpu_get(2 * sizeof(double));
-    const size_t hbytes = (2 * n + 2) * sizeof(double);
-    if (j->cap_host < hbytes) {
-        host_put(j->host_out);
-        j->host_out = (double *)host_get(hbytes);
-        j->cap_host = j->host_out ? hbytes : 0;
-    }
-    if (!j->out_d || !j->host_out) return fail(SDT_ERR_NOMEM, "sdt_job_run: output buffers");
-
-    int rc = cuda_check(cudaMemcpyAsync(j->klist_d, klist, 7 * n * sizeof(int64_t), cudaMemcpyHostToDevice, st), "sdt_job_run");
-    if (!rc) rc = cuda_check(cudaMemcpyAsync(j->pref_d, pref.data(), (n + 1) * sizeof(int64_t), cudaMemcpyHostToDevice, st), "sdt_job_run");
-    if (!rc) rc = cuda_check(cudaMemcpyAsync(j->factor_d, fac.data(), n * sizeof(double), cudaMemcpyHostToDevice, st), "sdt_job_run");
-    if (!rc && mixed)
-        rc = cuda_check(cudaMemcpyAsync(j->spref_d, spref.data(), (n + 1) * sizeof(int64_t), cudaMemcpyHostToDevice, st), "sdt_job_run");
-    if (rc) return rc;
-
-    if (mixed) {
-        if (j->mixed_type != mtype) {
-            rc = mixed_prepare(j, mtype, st);
-            if (rc) return rc;
-        }
-        if (j->timing) {
-            if (!j->ev0) cudaEventCreate(&j->ev0);
-            if (!j->ev1) cudaEventCreate(&j->ev1);
-            cudaEventRecord(j->ev0, st);
-        }
-        rc = mixed_launch(j, spref[n], n, st);
-        if (j->timing) cudaEventRecord(j->ev1, st);
-        if (rc) return rc;
-    } else {
-    FusedParams p;
-    p.T1d = j->arr[DST_T1]; p.T2a = j->arr[DST_T2A]; p.T2b = j->arr[DST_T2B];
-    p.Vd2 = j->arr[DST_VD2]; p.Wd1 = j->arr[DST_WD1]; p.Ud = j->arr[DST_UD];
-    p.pair_off = j->pair_off;
-    p.evl = j->evl_d;
-    p.tiles = j->tiles;
-    p.noab = (int32_t)t.noab; p.nvab = (int32_t)t.nvab;
-    p.nocc = t.nocc; p.nvir = t.nvir;
-    p.klist = j->klist_d; p.item_pref = j->pref_d; p.factor = j->factor_d;
-    p.n_tasks = n;
-    p.part = j->part_d;
-    const int64_t chunk = 1ll << 30;
-    if (j->timing) {
-        if (!j->ev0) cudaEventCreate(&j->ev0);
-        if (!j->ev1) cudaEventCreate(&j->ev1);
-        cudaEventRecord(j->ev0, st);
-    }
-    for (int64_t b0 = 0; b0 < items; b0 += chunk) {
-        p.item_base = b0;
-        const unsigned nb = (unsigned)std::min<int64_t>(chunk, items - b0);
-        fused_fp64_kernel<<<nb, kThreads, 0, st>>>(p);
-        count_launch();
-    }
-    if (j->timing) cudaEventRecord(j->ev1, st);
-    rc = cuda_check(cudaGetLastError(), "sdt_job_run: fused kernel");
-    if (rc) return rc;
-    }
-    rc = finish_run(j, n, st);
-    if (rc) return rc;
-    rc = cuda_check(cudaMemcpyAsync(j->host_out, j->out_d, 2 * sizeof(double), cudaMemcpyDeviceToHost, st), "sdt_job_run");
-    if (!rc && per_task)
-        rc = cuda_check(cudaMemcpyAsync(j->host_out + 2, j->task_d, 2 * n * sizeof(double), cudaMemcpyDeviceToHost, st), "sdt_job_run");
-    if (rc) return rc;
-    rc = cuda_check(cudaStreamSynchronize(st), "sdt_job_run");
-    if (rc) return rc;
-    if (j->timing) cudaEventElapsedTime(&j->last_ms, j->ev0, j->ev1);
-    if (mixed && j->err_h && *j->err_h)
-        return fail(SDT_ERR_TIMEOUT, "sdt_job_run: a bounded wait in the mixed kernel ran out (code " +
-                                         std::to_string(*j->err_h) + ")");
-    energy[0] = j->host_out[0];
-    energy[1] = j->host_out[1];
-    if (per_task) std::memcpy(per_task, j->host_out + 2, 2 * n * sizeof(double));
-    return SDT_OK;
-}
+}  // namespace sdt
 
 extern "C" int sdt_job_destroy(sdt_job *j) {
     if (!j) return SDT_OK;
@@ -816,14 +716,7 @@ extern "C" int sdt_job_destroy(sdt_job *j) {
     gpu_put(j->tiles);
     gpu_put(j->evl_d);
     gpu_put(j->pair_off);
-    gpu_put(j->klist_d);
-    gpu_put(j->pref_d);
-    gpu_put(j->spref_d);
-    gpu_put(j->factor_d);
-    gpu_put(j->part_d);
-    gpu_put(j->task_d);
-    gpu_put(j->out_d);
-    host_put(j->host_out);
+
     if (j->ev0) cudaEventDestroy(j->ev0);
     if (j->ev1) cudaEventDestroy(j->ev1);
     delete j;

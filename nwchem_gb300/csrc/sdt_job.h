@@ -39,15 +39,8 @@ struct sdt_job {
     int32_t nob = 0, nvb = 0;            // hole and particle boxes over all tiles
     int mixed_kseg = 0;                  // K chunks per TMEM drain (0: whole term)
     int mixed_cluster = 1;               // CTAs per cluster of the mixed kernel: 1 or 4
-    int *err_d = nullptr;
-    int *err_h = nullptr;                // pinned copy of err_d
+    int all_k = 1;                       // every K tile allowed for every term
     bool loaded = false;
-    // run workspace
-    int64_t *klist_d = nullptr, *pref_d = nullptr, *spref_d = nullptr;
-    double *factor_d = nullptr, *part_d = nullptr, *task_d = nullptr, *out_d = nullptr;
-    size_t cap_tasks = 0, cap_items = 0;
-    double *host_out = nullptr;
-    size_t cap_host = 0;
     // optional CUDA-event timing of the fused launches of the last run
     bool timing = false;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -56,16 +49,35 @@ struct sdt_job {
 
 
 namespace sdt {
-// Per-tuple compensated sums of the item partials, the total, into out_d.
-int finish_run(sdt_job *j, int64_t n, cudaStream_t st);
-// Frees the mixed-form operands and maps of a job.
+// Multiplicity factor of a tuple (ccsd_t_dot.F:52-66).
+double tuple_factor(const int64_t *k, bool restricted);
+
+// One persistent launch over a contiguous group of tuples.  Prefix arrays
+// are relative to the group: item_pref[q] (and, mixed form, super_pref[q],
+// the cluster work units) count from zero; part receives the group's item
+// pairs.
+struct LaunchArgs {
+    const int64_t *klist = nullptr, *item_pref = nullptr, *super_pref = nullptr;
+    const double *factor = nullptr;
+    double *part = nullptr;
+    int64_t n = 0, items = 0, n_super = 0;
+    unsigned long long *queue = nullptr;  // work counter, reset by the launch
+    int *err = nullptr;                   // mixed form: wait-timeout code, reset by the launch
+    int cluster = 1, grid = 1;
+};
+
+// Per-tuple compensated sums of item pairs (gpref: global item prefix, n+1)
+// into task (2n) and the compensated total into out (2).
+int tuple_sums(const double *part, const int64_t *gpref, int64_t n, double *task, double *out, cudaStream_t st);
+int fp64_grid(sdt_job *j, int64_t items, int *grid);
+int fp64_launch(sdt_job *j, const LaunchArgs &a, cudaStream_t st);
+// Frees the mixed-form operands of a job.
 void mixed_release(sdt_job *j);
-// Builds the split operands of element type `type` (TM_*) and the tensor
-// maps (after a successful load).
+// Builds the split operands of element type `type` (TM_*) and the box
+// tables (after a successful load).
 int mixed_prepare(sdt_job *j, int type, cudaStream_t st);
-// Launches the persistent mixed kernel over the n_super cluster work units
-// (super-item prefix in spref_d) of the n tuples.
-int mixed_launch(sdt_job *j, int64_t n_super, int64_t n, cudaStream_t st);
-int make_tmap(CUtensorMap *map, const void *base, int type, int rank, const uint64_t *dims,
-              const uint64_t *strides_bytes, const uint32_t *box, int swizzle_bytes);
+// Grid of the mixed kernel for a group (sets the kernel's shared-memory
+// attribute; call outside stream capture).
+int mixed_grid(sdt_job *j, int cluster, int64_t n_super, int *grid);
+int mixed_launch(sdt_job *j, const LaunchArgs &a, cudaStream_t st);
 }  // namespace sdt

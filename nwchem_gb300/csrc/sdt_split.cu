@@ -146,6 +146,8 @@ struct SplitParams {
     double inv_s, inv_s2;         // undo the operand scaling (FP16): X_true = X * inv_s
     double *part;
     int *err;
+    unsigned long long *queue;    // work-unit counter (single CTAs), zero at launch
+    int32_t all_k;                // every K tile allowed for every term (one spin, no irreps)
 };
 
 struct ItemBox {
@@ -200,6 +202,81 @@ __device__ __forceinline__ void decode_super(const SplitParams &p, int64_t si, i
     }
 }
 
+// K chunks of merged term td for one part (0: d1, K over occupied tiles;
+// 1: d2, K over virtual tiles).  A chunk (KE consecutive orbitals of the
+// space) is kept when it meets a K tile that spin and irrep allow for the
+// term -- the T2 read t(C0,C1;C2,m) for d1 and t(R0,e;R1,R2) for d2
+// (tce_hashnsort.F:31-36, :107-111); forbidden blocks are zero in the
+// operands, so a kept chunk that straddles one adds nothing.  f(c) is called
+// in increasing c; returns the count.
+template <int KE, class F>
+__device__ __forceinline__ int term_chunks(const SplitParams &p, const ItemBox &bx, const MergedTerm &td, int part,
+                                           F &&f) {
+    const int nk = part == 0 ? p.nk_o : p.nk_v;
+    if (p.all_k) {
+        for (int c = 0; c < nk; ++c) f(c);
+        return nk;
+    }
+    const int32_t *tl = p.tiles;
+    auto sp = [&](int d) { return __ldg(tl + 4 * (bx.tile[d] - 1) + 2); };
+    auto sy = [&](int d) { return __ldg(tl + 4 * (bx.tile[d] - 1) + 3); };
+    int need_s, need_y;  // spin and irrep the summed tile must have
+    if (part == 0) {
+        need_s = sp(td.c[0]) + sp(td.c[1]) - sp(td.c[2]);
+        need_y = sy(td.c[0]) ^ sy(td.c[1]) ^ sy(td.c[2]);
+    } else {
+        need_s = sp(td.r[1]) + sp(td.r[2]) - sp(td.r[0]);
+        need_y = sy(td.r[0]) ^ sy(td.r[1]) ^ sy(td.r[2]);
+    }
+    const int t0 = part == 0 ? 1 : p.noab + 1, t1 = part == 0 ? p.noab : p.noab + p.nvab;
+    int last = -1, n = 0;
+    for (int T = t0; T <= t1; ++T) {
+        if (__ldg(tl + 4 * (T - 1) + 2) != need_s || __ldg(tl + 4 * (T - 1) + 3) != need_y) continue;
+        const int st = __ldg(tl + 4 * (T - 1)), r = __ldg(tl + 4 * (T - 1) + 1);
+        const int c1 = (st + r - 1) / KE;
+        for (int c = max(st / KE, last + 1); c <= c1; ++c, ++n) f(c);
+        last = max(last, c1);
+    }
+    return n;
+}
+
+template <int KE>
+__device__ __forceinline__ int term_chunk_count(const SplitParams &p, const ItemBox &bx, int t) {
+    const MergedTerm td = kMerged[t];
+    return term_chunks<KE>(p, bx, td, 0, [](int) {}) + term_chunks<KE>(p, bx, td, 1, [](int) {});
+}
+
+// Drains (accumulator segments) of a term of nk kept chunks.
+__device__ __forceinline__ int term_segments(int nk, int kseg_req, int &kseg) {
+    kseg = (kseg_req > 0 && kseg_req < nk) ? kseg_req : (nk > 0 ? nk : 1);
+    return nk > 0 ? (nk + kseg - 1) / kseg : 1;
+}
+
+// Work units of a CTA.  Clusters (CS = 4) walk a fixed round-robin list;
+// single CTAs draw from the device queue: the producer thread takes the next
+// unit and publishes it in a 4-slot ring (id, or -1 at the end), which the MMA
+// thread, the drain leader and the energy leader each read and release.
+constexpr int SX_RING = 4;
+struct UnitRing {
+    int64_t *id;
+    uint64_t *full, *empty;
+};
+__device__ __forceinline__ bool ring_publish(const UnitRing &r, int n, int64_t u, volatile int *abort) {
+    const int s = n % SX_RING;
+    if (n >= SX_RING && !tc::mbar_wait(&r.empty[s], ((n / SX_RING) - 1) & 1, kWaitNs, abort)) return false;
+    r.id[s] = u;
+    tc::mbar_arrive(&r.full[s]);
+    return true;
+}
+// Returns the unit, -1 at the end, -2 when the wait ran out.
+__device__ __forceinline__ int64_t ring_take(const UnitRing &r, int n, volatile int *abort) {
+    const int s = n % SX_RING;
+    if (!tc::mbar_wait(&r.full[s], (n / SX_RING) & 1, kWaitNs, abort)) return -2;
+    const int64_t u = r.id[s];
+    tc::mbar_arrive(&r.empty[s]);
+    return u;
+}
+
 __device__ __forceinline__ void named_bar(int id, int n) {
     asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(n) : "memory");
 }
@@ -237,15 +314,28 @@ __device__ __forceinline__ void bulk_load_mc(void *dst, const void *src, uint32_
 template <int TYPE, int CS>
 __device__ __forceinline__ void run_producer(const SplitParams &p, uint8_t *stages, uint64_t *full,
                                              uint64_t *empty, volatile int *abort, int rj, int rk,
-                                             int64_t unit0, int64_t ustep) {
+                                             int64_t unit0, int64_t ustep, const UnitRing &ring) {
     constexpr int PJ = CS == 4 ? 2 : 1;
-    const int nk = p.nk_o + p.nk_v;
+    constexpr int KE = TYPE == TM_F32 ? 8 : 16;  // K values per 32-byte row
     const int rank = 2 * rj + rk;
     const uint16_t m_all = 0xF, m_rk = (uint16_t)((1u << rk) | (1u << (2 + rk))), m_rj = (uint16_t)(3u << (2 * rj));
     const int64_t NOB = p.nob, NVB = p.nvb;
     uint32_t g = 0;
     bool stop = false;
-    for (int64_t si = unit0; si < p.n_super && !stop; si += ustep) {
+    for (int n = 0; !stop; ++n) {
+        int64_t si;
+        if (CS == 1) {
+            const unsigned long long u = atomicAdd(p.queue, 1ull);
+            si = u < (unsigned long long)p.n_super ? (int64_t)u : -1;
+            if (!ring_publish(ring, n, si, abort)) {
+                stop = true;
+                break;
+            }
+            if (si < 0) break;
+        } else {
+            si = unit0 + (int64_t)n * ustep;
+            if (si >= p.n_super) break;
+        }
         ItemBox bx;
         decode_super<PJ>(p, si, rj, rk, bx);
         int gb[6];  // global box ids
@@ -254,7 +344,7 @@ __device__ __forceinline__ void run_producer(const SplitParams &p, uint8_t *stag
         for (int t = 0; t < 9 && !stop; ++t) {
             const MergedTerm td = kMerged[t];
             const int ty = t % 3;
-            // first blocks of the term's d1 and d2 parts (K chunk 0)
+            // first blocks (K chunk 0) of the term's d1 and d2 operands
             const int64_t arow = ((int64_t)gb[td.r[0]] * NOB + gb[td.r[1]]) * NOB + gb[td.r[2]];
             const int64_t a1 = arow * p.nk_o, a2 = arow * p.nk_v;
             const int64_t b1 = (((int64_t)gb[td.c[0]] * NVB + gb[td.c[1]]) * NOB + gb[td.c[2]]) * p.nk_o;
@@ -268,36 +358,39 @@ __device__ __forceinline__ void run_producer(const SplitParams &p, uint8_t *stag
             const int nbp = CS == 1 ? 1 : ty == 0 ? 4 : 2;
             const int hb = CS == 1 ? 0 : ty == 0 ? rank : ty == 1 ? rk : rj;
             const uint16_t mb = ty == 0 ? m_all : ty == 1 ? m_rj : m_rk;
-            for (int kc = 0; kc < nk; ++kc, ++g) {
-                const int s = g % SX_NS;
-                if (g >= SX_NS && !tc::mbar_wait(&empty[s], ((g / SX_NS) & 1) ^ 1, kWaitNs, abort)) {
-                    stop = true;
-                    break;
-                }
-                uint8_t *st = stages + s * SX_STAGE;
-                tc::mbar_arrive_expect_tx(&full[s], SX_STAGE);  // this CTA's whole stage, from all issuers
-                const bool d1 = kc < p.nk_o;
-                const int la = d1 ? L_WD1 : L_T2B, lb = d1 ? L_T2A : L_VD2;
-                const int64_t ab = d1 ? a1 + kc : a2 + (kc - p.nk_o);
-                const int64_t bb = d1 ? b1 + kc : b2 + (kc - p.nk_o);
-                const uint8_t *ah = p.blk[2 * la] + ab * SX_A, *al = p.blk[2 * la + 1] + ab * SX_A;
-                const uint8_t *bh = p.blk[2 * lb] + bb * SX_B, *bl = p.blk[2 * lb + 1] + bb * SX_B;
-                if (ha < 0) {
-                    bulk_load(st, ah, SX_A, &full[s]);
-                    bulk_load(st + SX_A, al, SX_A, &full[s]);
-                } else {
-                    const int off = ha * (SX_A / 2);
-                    bulk_load_mc(st + off, ah + off, SX_A / 2, &full[s], ma);
-                    bulk_load_mc(st + SX_A + off, al + off, SX_A / 2, &full[s], ma);
-                }
-                if (nbp == 1) {
-                    bulk_load(st + 2 * SX_A, bh, SX_B, &full[s]);
-                    bulk_load(st + 2 * SX_A + SX_B, bl, SX_B, &full[s]);
-                } else {
-                    const int piece = SX_B / nbp, off = hb * piece;
-                    bulk_load_mc(st + 2 * SX_A + off, bh + off, piece, &full[s], mb);
-                    bulk_load_mc(st + 2 * SX_A + SX_B + off, bl + off, piece, &full[s], mb);
-                }
+            for (int part = 0; part < 2 && !stop; ++part) {
+                const int la = part == 0 ? L_WD1 : L_T2B, lb = part == 0 ? L_T2A : L_VD2;
+                const int64_t abase = part == 0 ? a1 : a2, bbase = part == 0 ? b1 : b2;
+                term_chunks<KE>(p, bx, td, part, [&](int c) {
+                    if (stop) return;
+                    const int s = g % SX_NS;
+                    if (g >= SX_NS && !tc::mbar_wait(&empty[s], ((g / SX_NS) & 1) ^ 1, kWaitNs, abort)) {
+                        stop = true;
+                        return;
+                    }
+                    ++g;
+                    uint8_t *st = stages + s * SX_STAGE;
+                    tc::mbar_arrive_expect_tx(&full[s], SX_STAGE);  // this CTA's whole stage, from all issuers
+                    const int64_t ab = abase + c, bb = bbase + c;
+                    const uint8_t *ah = p.blk[2 * la] + ab * SX_A, *al = p.blk[2 * la + 1] + ab * SX_A;
+                    const uint8_t *bh = p.blk[2 * lb] + bb * SX_B, *bl = p.blk[2 * lb + 1] + bb * SX_B;
+                    if (ha < 0) {
+                        bulk_load(st, ah, SX_A, &full[s]);
+                        bulk_load(st + SX_A, al, SX_A, &full[s]);
+                    } else {
+                        const int off = ha * (SX_A / 2);
+                        bulk_load_mc(st + off, ah + off, SX_A / 2, &full[s], ma);
+                        bulk_load_mc(st + SX_A + off, al + off, SX_A / 2, &full[s], ma);
+                    }
+                    if (nbp == 1) {
+                        bulk_load(st + 2 * SX_A, bh, SX_B, &full[s]);
+                        bulk_load(st + 2 * SX_A + SX_B, bl, SX_B, &full[s]);
+                    } else {
+                        const int piece = SX_B / nbp, off = hb * piece;
+                        bulk_load_mc(st + 2 * SX_A + off, bh + off, piece, &full[s], mb);
+                        bulk_load_mc(st + 2 * SX_A + SX_B + off, bl + off, piece, &full[s], mb);
+                    }
+                });
             }
         }
     }
@@ -316,14 +409,28 @@ __device__ __forceinline__ void run_producer(const SplitParams &p, uint8_t *stag
 template <int TYPE, int CS>
 __device__ __forceinline__ void run_mma(const SplitParams &p, uint8_t *stages, uint64_t *full, uint64_t *empty,
                                         uint64_t *tfull, uint64_t *tempty, uint64_t *drain, uint32_t tmem,
-                                        volatile int *abort, int64_t unit0, int64_t ustep) {
-    const int nk = p.nk_o + p.nk_v;
-    const int kseg = p.kseg > 0 && p.kseg < nk ? p.kseg : nk;
-    const int nseg = (nk + kseg - 1) / kseg;
+                                        volatile int *abort, int rj, int rk, int64_t unit0, int64_t ustep,
+                                        const UnitRing &ring) {
+    constexpr int PJ = CS == 4 ? 2 : 1;
+    constexpr int KE = TYPE == TM_F32 ? 8 : 16;
     uint32_t g = 0, sg = 0;  // stage and segment counters
     bool stop = false;
-    for (int64_t si = unit0; si < p.n_super && !stop; si += ustep) {
+    for (int n = 0; !stop; ++n) {
+        int64_t si;
+        if (CS == 1) {
+            si = ring_take(ring, n, abort);
+            if (si == -2) stop = true;
+            if (si < 0) break;
+        } else {
+            si = unit0 + (int64_t)n * ustep;
+            if (si >= p.n_super) break;
+        }
+        ItemBox bx;
+        decode_super<PJ>(p, si, rj, rk, bx);
         for (int t = 0; t < 9 && !stop; ++t) {
+            const int nk = term_chunk_count<KE>(p, bx, t);
+            int kseg;
+            const int nseg = term_segments(nk, p.kseg, kseg);
             for (int sgi = 0; sgi < nseg && !stop; ++sgi, ++sg) {
                 const int buf = sg & 1;
                 if (sg >= 2 && !tc::mbar_wait(&tempty[buf], ((sg >> 1) - 1) & 1, kWaitNs, abort)) {
@@ -349,7 +456,7 @@ __device__ __forceinline__ void run_mma(const SplitParams &p, uint8_t *stages, u
                     if (CS == 4) tc::mma_commit_mc(&empty[s], 0xF);  // free here: tell all 4 CTAs
                     else tc::mma_commit(&empty[s]);
                 }
-                if (!stop) tc::mma_commit(&tfull[buf]);
+                if (!stop) tc::mma_commit(&tfull[buf]);  // an empty term commits nothing new
             }
         }
     }
@@ -523,14 +630,20 @@ __global__ void __launch_bounds__(SX_THREADS, 1) split_fused_kernel(const __grid
     uint8_t *misc = stages + SX_NS * SX_STAGE;
     uint64_t *bars = (uint64_t *)misc;
     uint64_t *full = bars, *empty = bars + SX_NS, *tfull = bars + 2 * SX_NS, *tempty = tfull + 2,
-             *drain = tempty + 2, *xready = drain + 1, *xfree = xready + 1;
-    uint32_t *tslot = (uint32_t *)(misc + 128);
-    volatile int *abort = (volatile int *)(misc + 132);
-    volatile int *dr_ok = (volatile int *)(misc + 136);
-    volatile int *en_ok = (volatile int *)(misc + 140);
-    EDesc *desc = (EDesc *)(misc + 256);
+             *drain = tempty + 2, *xready = drain + 1, *xfree = xready + 1, *ufull = xfree + 1,
+             *uempty = ufull + SX_RING;  // 23 barriers: 184 bytes
+    uint32_t *tslot = (uint32_t *)(misc + 192);
+    volatile int *abort = (volatile int *)(misc + 196);
+    volatile int *dr_ok = (volatile int *)(misc + 200);
+    volatile int *en_ok = (volatile int *)(misc + 204);
+    volatile int64_t *dr_unit = (volatile int64_t *)(misc + 208);
+    volatile int64_t *en_unit = (volatile int64_t *)(misc + 216);
+    int *dr_nk = (int *)(misc + 224);              // [9] kept K chunks per term of the drained item
+    EDesc *desc = (EDesc *)(misc + 320);
     double *red = (double *)(misc + 512);          // [8 energy warps][2]
+    const UnitRing ring{(int64_t *)(misc + 768), ufull, uempty};
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    constexpr int KE = TYPE == TM_F32 ? 8 : 16;
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < SX_NS; ++s) {
@@ -544,6 +657,10 @@ __global__ void __launch_bounds__(SX_THREADS, 1) split_fused_kernel(const __grid
         tc::mbar_init(drain, 1);
         tc::mbar_init(xready, 1);
         tc::mbar_init(xfree, 1);
+        for (int s = 0; s < SX_RING; ++s) {
+            tc::mbar_init(&ufull[s], 1);
+            tc::mbar_init(&uempty[s], 3);  // MMA thread, drain leader, energy leader
+        }
         *abort = 0;
         *dr_ok = 1;
         *en_ok = 1;
@@ -561,14 +678,12 @@ __global__ void __launch_bounds__(SX_THREADS, 1) split_fused_kernel(const __grid
     const int64_t unit0 = CS > 1 ? tc::cluster_id_x() : blockIdx.x;
     const int64_t ustep = CS > 1 ? tc::cluster_count_x() : gridDim.x;
 
-    const int nk = p.nk_o + p.nk_v;
-    const int kseg = p.kseg > 0 && p.kseg < nk ? p.kseg : nk;
-    const int nseg = (nk + kseg - 1) / kseg;
     if (warp < 4) {
         asm volatile("setmaxnreg.dec.sync.aligned.u32 %0;" ::"n"(SX_REG_LOW));
-        if (warp == 0 && lane == 0) run_producer<TYPE, CS>(p, stages, full, empty, abort, rj, rk, unit0, ustep);
+        if (warp == 0 && lane == 0)
+            run_producer<TYPE, CS>(p, stages, full, empty, abort, rj, rk, unit0, ustep, ring);
         else if (warp == 1 && lane == 0)
-            run_mma<TYPE, CS>(p, stages, full, empty, tfull, tempty, drain, tmem, abort, unit0, ustep);
+            run_mma<TYPE, CS>(p, stages, full, empty, tfull, tempty, drain, tmem, abort, rj, rk, unit0, ustep, ring);
     } else if (warp < 8) {
         // ---------------- drain warps ----------------
         asm volatile("setmaxnreg.dec.sync.aligned.u32 %0;" ::"n"(SX_REG_DRAIN));
@@ -577,10 +692,28 @@ __global__ void __launch_bounds__(SX_THREADS, 1) split_fused_kernel(const __grid
         const bool leader = (warp == 4 && lane == 0);
         const uint32_t tq = tmem + ((uint32_t)(quad * 32) << 16);
         uint32_t sg = 0;
-        int n = 0;  // items started by this CTA
         bool ok = true;
-        for (int64_t si = unit0; si < p.n_super && ok; si += ustep, ++n) {
+        for (int n = 0; ok; ++n) {
+            if (leader) {
+                int64_t si = CS == 1 ? ring_take(ring, n, abort) : unit0 + (int64_t)n * ustep;
+                if (CS > 1 && si >= p.n_super) si = -1;
+                if (si >= 0) {
+                    ItemBox bx;
+                    decode_super<PJ>(p, si, rj, rk, bx);
+                    for (int t = 0; t < 9; ++t) dr_nk[t] = term_chunk_count<KE>(p, bx, t);
+                }
+                *dr_unit = si;
+            }
+            named_bar(1, SX_DRAIN);
+            const int64_t si = *dr_unit;
+            if (si < 0) {
+                ok = si == -1;
+                break;
+            }
             for (int t = 0; t < 9 && ok; ++t) {
+                const int nk = dr_nk[t];
+                int kseg;
+                const int nseg = term_segments(nk, p.kseg, kseg);
                 for (int sgi = 0; sgi < nseg; ++sgi, ++sg) {
                     const int buf = sg & 1;
                     const bool first = (t == 0 && sgi == 0);
@@ -596,7 +729,11 @@ __global__ void __launch_bounds__(SX_THREADS, 1) split_fused_kernel(const __grid
                         break;
                     }
                     tc::tc_fence_after();
-                    drain_any(t, first, X, tq + (uint32_t)(buf * 256), m);
+                    if (nk > 0) {
+                        drain_any(t, first, X, tq + (uint32_t)(buf * 256), m);
+                    } else if (first) {  // no kept K chunk in the first term: start from zero
+                        for (int e = m * 256; e < m * 256 + 256; ++e) X[e] = 0.0f;
+                    }
                     tc::tc_fence_before();
                     named_bar(1, SX_DRAIN);
                     if (leader) {
@@ -620,28 +757,34 @@ __global__ void __launch_bounds__(SX_THREADS, 1) split_fused_kernel(const __grid
         const bool leader = (et == 0);
         float R[128];
         double e1 = 0.0, est = 0.0;
-        int n = 0;
-        for (int64_t si = unit0; si < p.n_super; si += ustep, ++n) {
+        for (int n = 0;; ++n) {
             if (leader) {
-                const bool w = tc::mbar_wait(xready, n & 1, kWaitNs, abort);
-                *en_ok = w ? 1 : 0;
-                if (w) {
-                    ItemBox bx;
-                    decode_super<PJ>(p, si, rj, rk, bx);
+                int64_t si = CS == 1 ? ring_take(ring, n, abort) : unit0 + (int64_t)n * ustep;
+                if (CS > 1 && si >= p.n_super) si = -1;
+                bool w = si != -2;
+                if (si >= 0) {
+                    w = tc::mbar_wait(xready, n & 1, kWaitNs, abort);
+                    if (w) {
+                        ItemBox bx;
+                        decode_super<PJ>(p, si, rj, rk, bx);
 #pragma unroll
-                    for (int dd = 0; dd < 6; ++dd) {
-                        desc->g[dd] = bx.start[dd] + bx.boff[dd];
-                        desc->nv[dd] = min(dd < 3 ? SX_BV : SX_BO, bx.ext[dd] - bx.boff[dd]);
+                        for (int dd = 0; dd < 6; ++dd) {
+                            desc->g[dd] = bx.start[dd] + bx.boff[dd];
+                            desc->nv[dd] = min(dd < 3 ? SX_BV : SX_BO, bx.ext[dd] - bx.boff[dd]);
+                        }
+                        desc->factor = p.factor[bx.tq];
+                        desc->item = bx.item;
                     }
-                    desc->factor = p.factor[bx.tq];
-                    desc->item = bx.item;
-                } else {
+                }
+                if (!w) {
                     *abort = 1;
                     atomicCAS(p.err, 0, 4);
+                    si = -2;
                 }
+                *en_unit = si;
             }
             named_bar(2, SX_EPI);
-            if (!*en_ok) break;
+            if (*en_unit < 0) break;
 #pragma unroll
             for (int A = 0; A < 4; ++A)
 #pragma unroll
@@ -812,12 +955,8 @@ void mixed_release(sdt_job *j) {
     gpu_put(j->t1f);
     gpu_put(j->uf);
     gpu_put(j->tile_box_d);
-    gpu_put(j->err_d);
-    host_put(j->err_h);
     j->t1f = j->uf = nullptr;
     j->tile_box_d = nullptr;
-    j->err_d = nullptr;
-    j->err_h = nullptr;
     j->mixed_type = -1;
 }
 
@@ -857,6 +996,10 @@ int mixed_prepare(sdt_job *j, int type, cudaStream_t st) {
     }
     j->inv_s = 1.0 / (sT * sI);
     j->inv_s2 = j->inv_s * j->inv_s;
+    // Every K tile is allowed for every term when all tiles share one spin and one irrep.
+    j->all_k = 1;
+    for (int64_t b = 2; b <= nt; ++b)
+        if (t.s(b) != t.s(1) || t.y(b) != t.y(1)) j->all_k = 0;
     // Box tables: global box ids per space, first index and valid rows.
     std::vector<int32_t> tile_box(nt), vrow0, vn, orow0, on;
     for (int64_t b = 1; b <= nt; ++b) {
@@ -908,9 +1051,7 @@ int mixed_prepare(sdt_job *j, int type, cudaStream_t st) {
     const size_t o_pblk0 = put64(pblk0), o_poff = put64(poff), o_pdim = put32(pdim);
     const size_t o_tbox = put32(tile_box), o_pairblk = put64(pair_blk);
     int64_t *tab_d = (int64_t *)gpu_get(std::max<size_t>(tab.size(), 1) * sizeof(int64_t));
-    j->err_d = (int *)gpu_get(sizeof(int));
-    j->err_h = (int *)host_get(sizeof(int));
-    if (!tab_d || !j->err_d || !j->err_h) {
+    if (!tab_d) {
         gpu_put(tab_d);
         mixed_release(j);
         return fail(SDT_ERR_NOMEM, "mixed form: tables");
@@ -989,7 +1130,48 @@ int mixed_prepare(sdt_job *j, int type, cudaStream_t st) {
     return SDT_OK;
 }
 
-int mixed_launch(sdt_job *j, int64_t n_super, int64_t n, cudaStream_t st) {
+int mixed_grid(sdt_job *j, int cluster, int64_t n_super, int *grid) {
+    auto setup = [&](auto kern) -> int {
+        int r = cuda_check(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, SX_SMEM_ALLOC),
+                           "mixed form: smem attribute");
+        if (r) return r;
+        if (cluster == 4) {
+            cudaLaunchAttribute attr[1];
+            attr[0].id = cudaLaunchAttributeClusterDimension;
+            attr[0].val.clusterDim.x = 4;
+            attr[0].val.clusterDim.y = 1;
+            attr[0].val.clusterDim.z = 1;
+            cudaLaunchConfig_t cfg = {};
+            cfg.blockDim = dim3(SX_THREADS);
+            cfg.dynamicSmemBytes = SX_SMEM_ALLOC;
+            cfg.attrs = attr;
+            cfg.numAttrs = 1;
+            cfg.gridDim = dim3(4);
+            int ncl = 0;
+            r = cuda_check(cudaOccupancyMaxActiveClusters(&ncl, kern, &cfg), "mixed form: cluster occupancy");
+            if (r) return r;
+            if (ncl < 1) return fail(SDT_ERR_CUDA, "mixed form: no cluster of 4 CTAs fits on this device");
+            *grid = (int)(4 * std::max<int64_t>(1, std::min<int64_t>(ncl, n_super)));
+        } else {
+            int nsm = 0;
+            r = cuda_check(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, j->dev), "mixed form");
+            if (r) return r;
+            *grid = (int)std::max<int64_t>(1, std::min<int64_t>(nsm, n_super));
+        }
+        return SDT_OK;
+    };
+    const int type = j->mixed_type;
+    if (cluster == 4) {
+        if (type == TM_F32) return setup(split_fused_kernel<TM_F32, 4>);
+        if (type == TM_BF16) return setup(split_fused_kernel<TM_BF16, 4>);
+        return setup(split_fused_kernel<TM_F16, 4>);
+    }
+    if (type == TM_F32) return setup(split_fused_kernel<TM_F32, 1>);
+    if (type == TM_BF16) return setup(split_fused_kernel<TM_BF16, 1>);
+    return setup(split_fused_kernel<TM_F16, 1>);
+}
+
+int mixed_launch(sdt_job *j, const LaunchArgs &a, cudaStream_t st) {
     const Tiling &t = j->t;
     const int type = j->mixed_type;
     const int ke = type == TM_F32 ? 8 : 16;
@@ -1010,21 +1192,19 @@ int mixed_launch(sdt_job *j, int64_t n_super, int64_t n, cudaStream_t st) {
     p.nob = j->nob;
     p.nvb = j->nvb;
     p.kseg = j->mixed_kseg;
-    p.klist = j->klist_d;
-    p.item_pref = j->pref_d;
-    p.super_pref = j->spref_d;
-    p.factor = j->factor_d;
-    p.n_tasks = n;
-    p.n_super = n_super;
+    p.klist = a.klist;
+    p.item_pref = a.item_pref;
+    p.super_pref = a.super_pref;
+    p.factor = a.factor;
+    p.n_tasks = a.n;
+    p.n_super = a.n_super;
     p.inv_s = j->inv_s;
     p.inv_s2 = j->inv_s2;
-    p.part = j->part_d;
-    p.err = j->err_d;
-    const bool cluster = j->mixed_cluster == 4;
-    auto launch = [&](auto kern) {
-        int r = cuda_check(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, SX_SMEM_ALLOC),
-                           "mixed form: smem attribute");
-        if (r) return r;
+    p.part = a.part;
+    p.err = a.err;
+    p.queue = a.queue;
+    p.all_k = j->all_k;
+    auto launch = [&](auto kern) -> int {
         cudaLaunchAttribute attr[1];
         attr[0].id = cudaLaunchAttributeClusterDimension;
         attr[0].val.clusterDim.x = 4;
@@ -1034,28 +1214,18 @@ int mixed_launch(sdt_job *j, int64_t n_super, int64_t n, cudaStream_t st) {
         cfg.blockDim = dim3(SX_THREADS);
         cfg.dynamicSmemBytes = SX_SMEM_ALLOC;
         cfg.stream = st;
-        if (cluster) {
+        cfg.gridDim = dim3((unsigned)a.grid);
+        if (a.cluster == 4) {
             cfg.attrs = attr;
             cfg.numAttrs = 1;
-            cfg.gridDim = dim3(4);
-            int ncl = 0;
-            r = cuda_check(cudaOccupancyMaxActiveClusters(&ncl, kern, &cfg), "mixed form: cluster occupancy");
-            if (r) return r;
-            if (ncl < 1) return fail(SDT_ERR_CUDA, "mixed form: no cluster of 4 CTAs fits on this device");
-            cfg.gridDim = dim3((unsigned)(4 * std::max<int64_t>(1, std::min<int64_t>(ncl, n_super))));
-        } else {
-            int nsm = 0;
-            r = cuda_check(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, j->dev), "mixed form");
-            if (r) return r;
-            cfg.gridDim = dim3((unsigned)std::max<int64_t>(1, std::min<int64_t>(nsm, n_super)));
         }
-        r = cuda_check(cudaLaunchKernelEx(&cfg, kern, p), "mixed form: fused kernel");
+        int r = cuda_check(cudaLaunchKernelEx(&cfg, kern, p), "mixed form: fused kernel");
         count_launch();
         return r;
     };
-    int rc = cuda_check(cudaMemsetAsync(j->err_d, 0, sizeof(int), st), "mixed form");
+    int rc = cuda_check(cudaMemsetAsync(a.queue, 0, sizeof(unsigned long long), st), "mixed form");
     if (rc) return rc;
-    if (cluster) {
+    if (a.cluster == 4) {
         if (type == TM_F32) rc = launch(split_fused_kernel<TM_F32, 4>);
         else if (type == TM_BF16) rc = launch(split_fused_kernel<TM_BF16, 4>);
         else rc = launch(split_fused_kernel<TM_F16, 4>);
@@ -1064,8 +1234,6 @@ int mixed_launch(sdt_job *j, int64_t n_super, int64_t n, cudaStream_t st) {
         else if (type == TM_BF16) rc = launch(split_fused_kernel<TM_BF16, 1>);
         else rc = launch(split_fused_kernel<TM_F16, 1>);
     }
-    if (!rc) rc = cuda_check(cudaMemcpyAsync(j->err_h, j->err_d, sizeof(int), cudaMemcpyDeviceToHost, st),
-                             "mixed form");
     return rc;
 }
 

@@ -92,6 +92,10 @@ def config_tiling(config: int, seed: int | None = None) -> Tiling:
     0: o=10, v=40, one tile each (seed 0)
     1: o=40 as 8/12/20, v=300 as 20,24x5,30x4,40 (seed 1)
     2: o=64 as 2x32, v=512 as 8x64 (seed 2)
+    3: blocked spatial symmetry: 8 occupied tiles (irreps 0..7) with lengths
+       drawn from {8,12,16,24,32} and 12 virtual tiles (irreps 0..7,0..3)
+       from {16,24,32,48,64}, drawn by numpy's PCG64 with seed 3; the
+       workload is the first 4096 tuples of the weight order (seed 3)
     """
     if config == 0:
         t = Tiling([10], [40], name="o10v40")
@@ -99,6 +103,12 @@ def config_tiling(config: int, seed: int | None = None) -> Tiling:
         t = Tiling([8, 12, 20], [20, 24, 24, 24, 24, 24, 30, 30, 30, 30, 40], name="o40v300")
     elif config == 2:
         t = Tiling([32, 32], [64] * 8, name="o64v512")
+    elif config == 3:
+        rng = np.random.default_rng(3)
+        occ = [int(x) for x in rng.choice([8, 12, 16, 24, 32], 8)]
+        vir = [int(x) for x in rng.choice([16, 24, 32, 48, 64], 12)]
+        t = Tiling(occ, vir, occ_sym=[q % 8 for q in range(8)], vir_sym=[q % 8 for q in range(12)],
+                   name="sym8_o%dv%d" % (sum(occ), sum(vir)))
     else:
         raise ValueError(f"no tiling for workload {config}")
     return t.with_evl(config if seed is None else seed)

@@ -175,3 +175,59 @@ def ccsd_t(tiling: Tiling, t1: TceFile, t2: TceFile, v2: TceFile) -> tuple[float
     _capi.check(lib.sdt_ccsd_t(C.byref(ts), C.byref(s[0]), C.byref(s[1]), C.byref(s[2]),
                                C.byref(e1), C.byref(e2)), "sdt_ccsd_t")
     return e1.value, e2.value
+
+
+class Plan:
+    """A prepared evaluation of a tuple list on a job (sdt_plan_*): host
+    indexing and uploads happen once; run() replays the captured CUDA graph
+    when capture() was called, else launches.  ctas (one per tuple, 1 or 4)
+    picks the mixed kernel's work-unit shape per tuple."""
+
+    def __init__(self, job: TriplesJob, klist: np.ndarray, precision: int = PREC_FP64, ctas=None):
+        self.job = job
+        self._lib = job._lib
+        self.klist = np.ascontiguousarray(klist, dtype=np.int64).reshape(-1, 7)
+        self.ctas = None if ctas is None else np.ascontiguousarray(ctas, dtype=np.int32)
+        if self.ctas is not None and len(self.ctas) != len(self.klist):
+            raise ValueError("one cluster size per tuple")
+        h = C.c_void_p()
+        _capi.check(self._lib.sdt_plan_create(
+            job._h, self.klist.ctypes.data_as(_capi.PI64), len(self.klist), int(precision),
+            None if self.ctas is None else self.ctas.ctypes.data_as(C.POINTER(C.c_int32)), C.byref(h)),
+            "sdt_plan_create")
+        self._h = h
+        self.precision = int(precision)
+
+    @property
+    def items(self) -> int:
+        return int(self._lib.sdt_plan_items(self._h))
+
+    def capture(self, stream=None) -> None:
+        _capi.check(self._lib.sdt_plan_capture(self._h, _stream_ptr(stream)), "sdt_plan_capture")
+
+    def launch(self, stream=None) -> None:
+        _capi.check(self._lib.sdt_plan_launch(self._h, _stream_ptr(stream)), "sdt_plan_launch")
+
+    def run(self, stream=None, per_task: bool = False):
+        e = np.zeros(2)
+        pt = np.zeros((len(self.klist), 2)) if per_task else None
+        _capi.check(self._lib.sdt_plan_run(self._h, _stream_ptr(stream), e.ctypes.data_as(_capi.PD),
+                                           pt.ctypes.data_as(_capi.PD) if per_task else None), "sdt_plan_run")
+        return (float(e[0]), float(e[1]), pt) if per_task else (float(e[0]), float(e[1]))
+
+    def close(self) -> None:
+        if self._h:
+            self._lib.sdt_plan_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

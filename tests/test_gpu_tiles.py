@@ -77,7 +77,8 @@ def test_each_tile_kernel_matches_oracle(lib, family, dims):
         scale = np.abs(want).max()
         assert scale > 0
         assert np.abs(got - want).max() <= 1e-13 * scale, (family, k, dims)
-    assert _capi.last_error()[0] == 0
+    code, msg = _capi.last_error()
+    assert code == 0, msg
 
 
 def _drive_tuple(lib, P, t, tup):
