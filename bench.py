@@ -463,6 +463,60 @@ def workload_sym8(args) -> None:
     print(json.dumps(out), flush=True)
 
 
+def workload_serve(args) -> None:
+    """Serving stream: Poisson arrivals at 50 jobs/s, o ~ U{omin..omax},
+    v = round(o * U[5,8]), tiles from {8..32} / {16..64} (no irreps),
+    inputs seeded with the job id; FIFO admission against a 150 GB HBM
+    budget on `slots` workers; the mixed form (FP16x3) on every job and the
+    FP64 form as a check on 1% of them.  Inputs are generated before the
+    stream starts; a job's latency runs from its arrival (submission) to
+    its energies."""
+    import torch
+
+    import nwchem_gb300 as ng
+    from nwchem_gb300 import serve
+    torch.cuda.set_device(0)
+    specs = serve.job_stream(args.jobs, 50.0, 4, args.omin, args.omax)
+    t0 = time.perf_counter()
+    files = serve.prepare(specs)
+    gen_s = time.perf_counter() - t0
+    prec = ng.PREC_MIXED_FP16
+    budget = 150 * 10**9
+    check = [s.id % 100 == 0 for s in specs]
+    with serve.Server(budget, slots=args.slots, max_ctas=args.max_ctas) as srv:
+        # warm-up job (kernel attributes, first allocations), not counted
+        w = srv.submit(specs[0].tiling, files[0], prec)
+        srv.drain(600)
+        t_start = time.perf_counter()
+        tickets = []
+        for s, f, c in zip(specs, files, check):
+            delay = s.arrival - (time.perf_counter() - t_start)
+            if delay > 0:
+                time.sleep(delay)
+            tickets.append(srv.submit(s.tiling, f, prec, check_fp64=c))
+        srv.drain(3600)
+        st = [srv.status(t) for t in tickets]
+        peak = srv.peak_bytes
+    ok = [x for x in st if x["state"] == 2]
+    lat = np.array([x["finished"] - x["submitted"] for x in ok])
+    span = max(x["finished"] for x in ok) - min(x["submitted"] for x in ok)
+    flops = sum(ng.flops(s.tiling, ng.task_list(s.tiling)) for s, x in zip(specs, st) if x["state"] == 2)
+    chk = [x for x, c in zip(st, check) if c and x["state"] == 2]
+    errs = [abs(x["energy"][1] - x["fp64"][1]) / abs(x["fp64"][1]) for x in chk if x["fp64"][1] != 0.0]
+    aerr = [abs(x["energy"][1] - x["fp64"][1]) for x in chk]
+    empty = sum(1 for s in specs if len(ng.task_list(s.tiling)) == 0)
+    print(json.dumps({
+        "workload": f"serving: {args.jobs} jobs, Poisson 50 jobs/s, o ~ U{{{args.omin}..{args.omax}}}, "
+                    f"v = round(o*U[5,8]), tiles {{8..32}}/{{16..64}}, seed = job id",
+        "slots": args.slots, "max_ctas": args.max_ctas, "budget_bytes": budget, "peak_admitted_bytes": peak,
+        "jobs_done": len(ok), "jobs_failed": len(st) - len(ok),
+        "jobs_per_s": len(ok) / span, "span_s": span, "p50_latency_s": float(np.percentile(lat, 50)),
+        "p99_latency_s": float(np.percentile(lat, 99)), "mean_latency_s": float(lat.mean()),
+        "tflops": flops / span / 1e12, "fp64_checked": len(chk), "jobs_without_tuples": empty,
+        "max_rel_err_E(T)_vs_fp64": max(errs) if errs else None, "max_abs_err_E(T)_vs_fp64_Eh": max(aerr) if aerr else None,
+        "input_generation_s": gen_s}), flush=True)
+
+
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -472,7 +526,12 @@ def main() -> None:
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--profile", action="store_true", help="small single-launch case for ncu")
     ap.add_argument("--tuples", type=int, default=2, help="tuples in the --profile case")
-    ap.add_argument("--workload", default="o40v300", choices=["o40v300", "o64v512", "sym8"])
+    ap.add_argument("--workload", default="o40v300", choices=["o40v300", "o64v512", "sym8", "serve"])
+    ap.add_argument("--jobs", type=int, default=200, help="serve: jobs in the stream")
+    ap.add_argument("--omin", type=int, default=8, help="serve: smallest occupied size")
+    ap.add_argument("--omax", type=int, default=24, help="serve: largest occupied size")
+    ap.add_argument("--slots", type=int, default=4, help="serve: worker slots")
+    ap.add_argument("--max-ctas", type=int, default=0, help="serve: CTA cap per job launch (0: all SMs)")
     ap.add_argument("--case", default="o40v114", choices=["o40v114", "o64v128"], help="--profile case")
     ap.add_argument("--kseg", type=int, default=0, help="mixed form: K chunks per accumulator drain")
     ap.add_argument("--mixed", default="", choices=["", "tf32", "bf16", "fp16"],
@@ -486,6 +545,8 @@ def main() -> None:
         workload_o64v512(args)
     elif args.workload == "sym8":
         workload_sym8(args)
+    elif args.workload == "serve":
+        workload_serve(args)
     elif args.profile:
         profile_case(args)
     elif args.impl == "reference":

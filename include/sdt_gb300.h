@@ -261,6 +261,47 @@ int sdt_plan_destroy(sdt_plan *plan);
 /* Sub-box work items of a plan. */
 int64_t sdt_plan_items(const sdt_plan *plan);
 
+/* Serving (no reference counterpart): a loop of independent (T) jobs on
+ * one GPU.  Jobs wait in one FIFO queue and are admitted when one of
+ * `slots` workers is free and sdt_job_bytes of the job fits in the byte
+ * budget minus the admitted jobs' bytes (a job larger than the budget
+ * fails with SDT_ERR_NOMEM); each admitted job runs on its own stream --
+ * create, load, the given precision over all its tuples, optionally the
+ * FP64 form as a check -- so admitted jobs overlap on the device.
+ * max_ctas (0: all SMs) caps the CTAs of each job's persistent launches.
+ * The caller keeps a job's files alive until its state is 2 (done) or -1
+ * (failed).  Times are seconds since sdt_server_create. */
+typedef struct sdt_server sdt_server;
+int sdt_server_create(int64_t budget_bytes, int slots, int max_ctas,
+                      sdt_server **server);
+int sdt_server_submit(sdt_server *server, const sdt_tiling *t,
+                      const sdt_file *t1, const sdt_file *t2,
+                      const sdt_file *v2, int precision, int check_fp64,
+                      int64_t *ticket);
+/* state 0 queued, 1 running, 2 done, -1 failed (the job's error code is
+ * returned and its message copied to msg); energy[2], fp64[2] (check) and
+ * times[3] (submitted, admitted, finished) may be NULL. */
+int sdt_server_status(sdt_server *server, int64_t ticket, int *state,
+                      double *energy, double *fp64, double *times,
+                      char *msg, size_t len);
+int sdt_server_drain(sdt_server *server, double timeout_s);
+int64_t sdt_server_peak_bytes(sdt_server *server);
+int sdt_server_destroy(sdt_server *server);
+/* Device bytes a job of this tiling needs at its peak (admission bound). */
+int64_t sdt_job_bytes(const sdt_tiling *t, int precision);
+/* The admission policy alone, simulated on the host: jobs arriving at
+ * arrival[q] (ascending) with bytes[q] and run times service[q]; start[q]
+ * and end[q] receive admission and completion times (-1: larger than the
+ * budget). */
+int sdt_admission_simulate(int64_t n, const double *arrival,
+                           const int64_t *bytes, const double *service,
+                           int64_t budget, int slots, double *start,
+                           double *end);
+/* Caps the CTAs of a job's persistent launches (0: all SMs). */
+int sdt_job_set_max_ctas(sdt_job *job, int ctas);
+/* The job's own stream (the default stream of its calls). */
+void *sdt_job_stream(const sdt_job *job);
+
 /* One-shot replacement for ccsd_t(d_t1,k_t1_offset,d_t2,k_t2_offset,
  * d_v2,k_v2_offset,energy1,energy2,size_t1) (ccsd_t.F:19-20): builds the
  * tuple list, loads the files, runs every tuple and returns E[T] in

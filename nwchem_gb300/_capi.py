@@ -67,6 +67,18 @@ def _declare(lib):
         "sdt_plan_run": (C.c_int, [C.c_void_p, C.c_void_p, PD, PD]),
         "sdt_plan_destroy": (C.c_int, [C.c_void_p]),
         "sdt_plan_items": (C.c_int64, [C.c_void_p]),
+        "sdt_server_create": (C.c_int, [C.c_int64, C.c_int, C.c_int, C.POINTER(C.c_void_p)]),
+        "sdt_server_submit": (C.c_int, [C.c_void_p, C.POINTER(SdtTiling), C.POINTER(SdtFile), C.POINTER(SdtFile),
+                                        C.POINTER(SdtFile), C.c_int, C.c_int, C.POINTER(C.c_int64)]),
+        "sdt_server_status": (C.c_int, [C.c_void_p, C.c_int64, C.POINTER(C.c_int), PD, PD, PD, C.c_char_p,
+                                        C.c_size_t]),
+        "sdt_server_drain": (C.c_int, [C.c_void_p, C.c_double]),
+        "sdt_server_peak_bytes": (C.c_int64, [C.c_void_p]),
+        "sdt_server_destroy": (C.c_int, [C.c_void_p]),
+        "sdt_job_bytes": (C.c_int64, [C.POINTER(SdtTiling), C.c_int]),
+        "sdt_admission_simulate": (C.c_int, [C.c_int64, PD, PI64, PD, C.c_int64, C.c_int, PD, PD]),
+        "sdt_job_set_max_ctas": (C.c_int, [C.c_void_p, C.c_int]),
+        "sdt_job_stream": (C.c_void_p, [C.c_void_p]),
         "sdt_tc_selftest": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]),
         "sdt_tc_selftest16": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int,
                                         C.c_void_p]),

@@ -20,7 +20,7 @@ LIB = LIBDIR / "libsdt_gb300.so"
 BUILD = PKG / "_build"
 
 SOURCES = ["sdt_host.cpp", "sdt_mem.cu", "sdt_tile.cu", "sdt_fused.cu", "sdt_probe.cu", "sdt_noalloc.cu", "sdt_mixed.cu",
-           "sdt_split.cu", "sdt_plan.cu"]
+           "sdt_split.cu", "sdt_plan.cu", "sdt_serve.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

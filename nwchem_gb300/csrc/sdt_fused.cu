@@ -389,7 +389,9 @@ int fp64_grid(sdt_job *j, int64_t items, int *grid) {
     if (!rc) rc = cuda_check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fused_fp64_kernel, kThreads, 0),
                              "FP64 form");
     if (rc) return rc;
-    *grid = (int)std::max<int64_t>(1, std::min<int64_t>(items, (int64_t)nsm * std::max(per_sm, 1)));
+    int64_t cap = (int64_t)nsm * std::max(per_sm, 1);
+    if (j->max_ctas > 0) cap = std::min<int64_t>(cap, (int64_t)j->max_ctas * std::max(per_sm, 1));
+    *grid = (int)std::max<int64_t>(1, std::min<int64_t>(items, cap));
     return SDT_OK;
 }
 
@@ -483,11 +485,12 @@ extern "C" int sdt_job_create(const sdt_tiling *ti, sdt_job **out) {
     j->t.alpha = j->alpha.empty() ? nullptr : j->alpha.data();
     j->t.evl = j->evl.data();
     cudaGetDevice(&j->dev);
-    cudaStream_t st = lib_stream();
-    if (!st) {
+    if (cudaStreamCreateWithFlags(&j->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        cudaGetLastError();
         delete j;
         return fail(SDT_ERR_CUDA, "sdt_job_create: no stream");
     }
+    cudaStream_t st = j->stream;
     int rc = tiles_upload(j, st);
     if (rc) {
         sdt_job_destroy(j);
@@ -508,7 +511,7 @@ extern "C" int sdt_job_load(sdt_job *j, const sdt_file *f1, const sdt_file *f2,
                             const sdt_file *fv, void *stream) {
     if (!j || !f1 || !f2 || !fv || !f1->hash || !f2->hash || !fv->hash)
         return fail(SDT_ERR_ARG, "sdt_job_load: null argument");
-    cudaStream_t st = stream ? (cudaStream_t)stream : lib_stream();
+    cudaStream_t st = stream ? (cudaStream_t)stream : j->stream;
     const Tiling &t = j->t;
     const int64_t o = t.nocc, v = t.nvir, noab = t.noab, nvab = t.nvab, N = noab + nvab;
 
@@ -710,7 +713,7 @@ double tuple_factor(const int64_t *k, bool restricted) {
 
 extern "C" int sdt_job_destroy(sdt_job *j) {
     if (!j) return SDT_OK;
-    cudaStreamSynchronize(lib_stream());
+    cudaStreamSynchronize(j->stream);
     job_free_arrays(j);
     mixed_release(j);
     gpu_put(j->tiles);
@@ -719,6 +722,7 @@ extern "C" int sdt_job_destroy(sdt_job *j) {
 
     if (j->ev0) cudaEventDestroy(j->ev0);
     if (j->ev1) cudaEventDestroy(j->ev1);
+    if (j->stream) cudaStreamDestroy(j->stream);
     delete j;
     return SDT_OK;
 }
@@ -751,6 +755,14 @@ extern "C" int sdt_job_set_timing(sdt_job *j, int on) {
 }
 
 extern "C" double sdt_job_last_kernel_ms(const sdt_job *j) { return j ? (double)j->last_ms : -1.0; }
+
+extern "C" int sdt_job_set_max_ctas(sdt_job *j, int sms) {
+    if (!j || sms < 0) return fail(SDT_ERR_ARG, "sdt_job_set_max_ctas: bad argument");
+    j->max_ctas = sms;
+    return SDT_OK;
+}
+
+extern "C" void *sdt_job_stream(const sdt_job *j) { return j ? (void *)j->stream : nullptr; }
 
 extern "C" int sdt_job_set_mixed_cluster(sdt_job *j, int ctas) {
     if (!j || (ctas != 1 && ctas != 4)) return fail(SDT_ERR_ARG, "sdt_job_set_mixed_cluster: 1 or 4 CTAs");

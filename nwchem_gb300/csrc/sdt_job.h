@@ -19,6 +19,8 @@ struct sdt_job {
     std::vector<int64_t> range, spin, sym, offset, alpha;
     std::vector<double> evl;
     int dev = 0;
+    cudaStream_t stream = nullptr;       // the job's own stream (default for its work)
+    int max_ctas = 0;                    // cap on the CTAs of its persistent launches (0: all SMs)
     // device
     int32_t *tiles = nullptr;
     double *evl_d = nullptr;

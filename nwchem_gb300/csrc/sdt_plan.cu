@@ -154,7 +154,7 @@ int plan_create(sdt_job *j, const int64_t *klist, int64_t n, int precision, cons
         if (!j->ev1 && cudaEventCreate(&j->ev1) != cudaSuccess) j->ev1 = nullptr;
         cudaGetLastError();
     }
-    cudaStream_t st = lib_stream();
+    cudaStream_t st = j->stream;
     int rc = SDT_OK;
     if (mixed) {
         p->mtype = mixed_type_of(precision);
@@ -263,12 +263,12 @@ extern "C" int sdt_plan_create(sdt_job *job, const int64_t *klist, int64_t n, in
 
 extern "C" int sdt_plan_launch(sdt_plan *plan, void *stream) {
     if (!plan) return fail(SDT_ERR_ARG, "sdt_plan_launch: null plan");
-    return plan_enqueue(plan, stream ? (cudaStream_t)stream : lib_stream());
+    return plan_enqueue(plan, stream ? (cudaStream_t)stream : plan->job->stream);
 }
 
 extern "C" int sdt_plan_capture(sdt_plan *plan, void *stream) {
     if (!plan) return fail(SDT_ERR_ARG, "sdt_plan_capture: null plan");
-    cudaStream_t st = stream ? (cudaStream_t)stream : lib_stream();
+    cudaStream_t st = stream ? (cudaStream_t)stream : plan->job->stream;
     if (plan->exec) {
         cudaGraphExecDestroy(plan->exec);
         plan->exec = nullptr;
@@ -294,7 +294,7 @@ extern "C" int sdt_plan_capture(sdt_plan *plan, void *stream) {
 
 extern "C" int sdt_plan_run(sdt_plan *plan, void *stream, double *energy, double *per_task) {
     if (!plan || !energy) return fail(SDT_ERR_ARG, "sdt_plan_run: null argument");
-    cudaStream_t st = stream ? (cudaStream_t)stream : lib_stream();
+    cudaStream_t st = stream ? (cudaStream_t)stream : plan->job->stream;
     int rc;
     if (plan->exec) {
         if (plan->mtype >= 0 && plan->job->mixed_type != plan->mtype)
@@ -310,7 +310,7 @@ extern "C" int sdt_plan_run(sdt_plan *plan, void *stream, double *energy, double
 
 extern "C" int sdt_plan_destroy(sdt_plan *plan) {
     if (!plan) return SDT_OK;
-    cudaStreamSynchronize(lib_stream());
+    cudaStreamSynchronize(plan->job->stream);
     plan_free(plan);
     return SDT_OK;
 }
@@ -324,7 +324,7 @@ extern "C" int sdt_job_run(sdt_job *j, const int64_t *klist, int64_t n, int prec
     sdt_plan *p = nullptr;
     int rc = plan_create(j, klist, n, precision, nullptr, &p, "sdt_job_run");
     if (rc) return rc;
-    cudaStream_t st = stream ? (cudaStream_t)stream : lib_stream();
+    cudaStream_t st = stream ? (cudaStream_t)stream : j->stream;
     rc = plan_enqueue(p, st);
     if (!rc) rc = plan_read(p, st, energy, per_task, "sdt_job_run");
     else cudaStreamSynchronize(st);

@@ -1,0 +1,359 @@
+// sdt_serve.cpp -- a serving loop for independent (T) jobs on one GPU (no
+// reference counterpart: NWChem evaluates one (T) problem per run).
+//
+// Clients submit jobs (a tiling and its T1/T2/V2 files) at any time.  Jobs
+// wait in one FIFO queue; a job is admitted when one of the server's slots
+// is free and its device bytes fit in the HBM budget minus the bytes of the
+// jobs already admitted (a job larger than the whole budget is rejected).
+// Each slot is a worker thread; an admitted job runs on its own CUDA stream:
+// device tables, H2D copy and ingest of its files, the mixed form's operand
+// encoding, the persistent kernel over all its tuples and the energy sums,
+// then (optionally) the FP64 form as a check, and its memory is returned.
+// Jobs admitted together overlap on the device -- one job's copies and
+// encoding with another's contraction kernel, and their kernels at launch
+// boundaries (or throughout, with max_ctas capping each job's CTAs).  A
+// job's result depends only on its inputs, never on what ran beside it.
+#include "sdt_internal.h"
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <memory>
+#include <mutex>
+#include <thread>
+#include <vector>
+
+namespace sdt {
+namespace {
+
+// FIFO admission against slots and a byte budget (the server and
+// sdt_admission_simulate share it).
+struct Admission {
+    int64_t budget = 0, in_use = 0, peak = 0;
+    int slots = 1, busy = 0;
+    bool fits_ever(int64_t bytes) const { return bytes <= budget; }
+    bool can_admit(int64_t bytes) const { return busy < slots && in_use + bytes <= budget; }
+    void admit(int64_t bytes) {
+        ++busy;
+        in_use += bytes;
+        peak = std::max(peak, in_use);
+    }
+    void release(int64_t bytes) {
+        --busy;
+        in_use -= bytes;
+    }
+};
+
+int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
+
+}  // namespace
+
+// Device bytes a job needs at its peak (an upper bound of the allocations of
+// sdt_job_create/load/run): the dense FP64 operands, the raw files during
+// ingest, for a mixed precision the split block layouts and FP32 copies, and
+// the run's partial sums.
+int64_t job_bytes(const sdt_tiling *ti, int precision) {
+    Tiling t;
+    if (!make_tiling(ti, &t)) return -1;
+    const int64_t o = t.nocc, v = t.nvir, N = t.noab + t.nvab;
+    int64_t vd2 = 0, vd2_blocks_pairs = 0, nob = 0, nvb = 0;
+    for (int64_t b = 1; b <= t.noab; ++b) nob += ceil_div(t.r(b), 4);
+    for (int64_t b = t.noab + 1; b <= N; ++b) nvb += ceil_div(t.r(b), 8);
+    for (int64_t B = t.noab + 1; B <= N; ++B)
+        for (int64_t C = B; C <= N; ++C) {
+            vd2 += t.r(B) * t.r(C) * o * v;
+            vd2_blocks_pairs += ceil_div(t.r(B), 8) * ceil_div(t.r(C), 8);
+        }
+    int64_t bytes = 8 * (v * o + 3 * v * v * o * o + vd2 + v * o * o * o);
+    // raw TCE files (canonical blocks: at most the dense sizes) during ingest
+    bytes += 8 * (v * o + v * v * o * o + vd2 + v * o * o * o + v * v * o * o);
+    int64_t items = 0;
+    const int64_t n = sdt_tasks_count(ti);
+    if (n > 0) {
+        std::vector<int64_t> kl(7 * n);
+        if (sdt_tasks_list(ti, n, kl.data()) == SDT_OK) {
+            const int bv = precision == SDT_PREC_FP64 ? 4 : 8;
+            for (int64_t q = 0; q < n; ++q) {
+                int64_t boxes = 1;
+                for (int d = 0; d < 6; ++d) boxes *= ceil_div(t.r(kl[7 * q + d]), d < 3 ? bv : 4);
+                items += boxes;
+            }
+        }
+        bytes += 16 * items + 64 * n;
+    }
+    if (precision != SDT_PREC_FP64) {
+        const int64_t es = precision == SDT_PREC_MIXED_TF32 ? 4 : 2, ke = 32 / es;
+        const int64_t nko = ceil_div(o, ke), nkv = ceil_div(v, ke);
+        const int64_t blocks_a = nvb * nob * nob * (nko + nkv);
+        const int64_t blocks_b = nvb * nvb * nob * nko + vd2_blocks_pairs * nob * nkv;
+        bytes += 2 * (blocks_a * 4096 + blocks_b * 8192);
+        bytes += 4 * (v * o + v * v * o * o);
+    }
+    return bytes + bytes / 20 + (64ll << 20);
+}
+
+}  // namespace sdt
+
+using namespace sdt;
+
+struct sdt_server {
+    struct Job {
+        int64_t id = 0;
+        std::vector<int64_t> range, spin, sym, offset, alpha;
+        std::vector<double> evl;
+        sdt_tiling t{};
+        sdt_file f1{}, f2{}, fv{};
+        int precision = SDT_PREC_MIXED_FP16, check = 0;
+        int64_t bytes = 0;
+        int state = 0;  // 0 queued, 1 running, 2 done, -1 failed
+        double e[2] = {0, 0}, f[2] = {0, 0};
+        double t_submit = 0, t_start = 0, t_end = 0;
+        int err = 0;
+        std::string msg;
+    };
+    int64_t budget = 0;
+    int slots = 1, max_ctas = 0;
+    std::mutex mu;
+    std::condition_variable cv;
+    std::deque<Job *> queue;
+    std::vector<std::unique_ptr<Job>> jobs;
+    Admission adm;
+    std::vector<std::thread> workers;
+    bool stop = false;
+    int device = 0;
+    std::chrono::steady_clock::time_point t0 = std::chrono::steady_clock::now();
+    double now() const {
+        return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    }
+};
+
+namespace {
+
+void run_one(sdt_server *s, sdt_server::Job *job) {
+    cudaSetDevice(s->device);
+    sdt_job *j = nullptr;
+    auto failed = [&](int rc) {
+        char buf[512] = {0};
+        sdt_last_error(buf, sizeof(buf));
+        job->err = rc;
+        job->msg = buf;
+        return rc;
+    };
+    int rc = sdt_job_create(&job->t, &j);
+    if (rc) {
+        failed(rc);
+        return;
+    }
+    if (s->max_ctas > 0) sdt_job_set_max_ctas(j, s->max_ctas);
+    rc = sdt_job_load(j, &job->f1, &job->f2, &job->fv, nullptr);
+    std::vector<int64_t> kl;
+    int64_t n = 0;
+    if (!rc) {
+        n = sdt_tasks_count(&job->t);
+        kl.resize(7 * std::max<int64_t>(n, 1));
+        rc = n < 0 ? SDT_ERR_ARG : sdt_tasks_list(&job->t, n, kl.data());
+    }
+    if (!rc) rc = sdt_job_run(j, kl.data(), n, job->precision, job->e, nullptr, nullptr);
+    if (!rc && job->check) rc = sdt_job_run(j, kl.data(), n, SDT_PREC_FP64, job->f, nullptr, nullptr);
+    if (rc) failed(rc);
+    sdt_job_destroy(j);
+}
+
+void worker(sdt_server *s) {
+    std::unique_lock<std::mutex> lk(s->mu);
+    while (true) {
+        s->cv.wait(lk, [&] {
+            return s->stop || (!s->queue.empty() && (!s->adm.fits_ever(s->queue.front()->bytes) ||
+                                                     s->adm.can_admit(s->queue.front()->bytes)));
+        });
+        if (s->stop) return;
+        sdt_server::Job *job = s->queue.front();
+        s->queue.pop_front();
+        if (!s->adm.fits_ever(job->bytes)) {
+            job->state = -1;
+            job->err = SDT_ERR_NOMEM;
+            job->msg = "sdt_server: the job needs more device memory than the whole budget";
+            job->t_start = job->t_end = s->now();
+            s->cv.notify_all();
+            continue;
+        }
+        s->adm.admit(job->bytes);
+        job->state = 1;
+        job->t_start = s->now();
+        lk.unlock();
+        run_one(s, job);
+        lk.lock();
+        s->adm.release(job->bytes);
+        job->t_end = s->now();
+        job->state = job->err ? -1 : 2;
+        s->cv.notify_all();
+    }
+}
+
+}  // namespace
+
+extern "C" int64_t sdt_job_bytes(const sdt_tiling *t, int precision) {
+    if (!t || precision < SDT_PREC_FP64 || precision > SDT_PREC_MIXED_FP16) return -1;
+    return job_bytes(t, precision);
+}
+
+extern "C" int sdt_server_create(int64_t budget_bytes, int slots, int max_ctas, sdt_server **out) {
+    if (!out || budget_bytes <= 0 || slots < 1 || slots > 64 || max_ctas < 0)
+        return fail(SDT_ERR_ARG, "sdt_server_create: bad argument");
+    sdt_server *s = new sdt_server();
+    s->budget = budget_bytes;
+    s->slots = slots;
+    s->max_ctas = max_ctas;
+    s->adm.budget = budget_bytes;
+    s->adm.slots = slots;
+    cudaGetDevice(&s->device);
+    for (int k = 0; k < slots; ++k) s->workers.emplace_back(worker, s);
+    *out = s;
+    return SDT_OK;
+}
+
+extern "C" int sdt_server_submit(sdt_server *s, const sdt_tiling *t, const sdt_file *t1, const sdt_file *t2,
+                                 const sdt_file *v2, int precision, int check_fp64, int64_t *ticket) {
+    if (!s || !t || !t1 || !t2 || !v2 || !ticket) return fail(SDT_ERR_ARG, "sdt_server_submit: null argument");
+    if (precision < SDT_PREC_FP64 || precision > SDT_PREC_MIXED_FP16)
+        return fail(SDT_ERR_ARG, "sdt_server_submit: unknown precision");
+    Tiling tt;
+    if (!make_tiling(t, &tt)) return fail(SDT_ERR_ARG, "sdt_server_submit: bad tiling");
+    auto job = std::make_unique<sdt_server::Job>();
+    const int64_t nt = t->noab + t->nvab;
+    job->range.assign(t->range, t->range + nt);
+    job->spin.assign(t->spin, t->spin + nt);
+    job->sym.assign(t->sym, t->sym + nt);
+    job->offset.assign(t->offset, t->offset + nt);
+    if (t->alpha) job->alpha.assign(t->alpha, t->alpha + nt);
+    job->evl.assign(t->evl_sorted, t->evl_sorted + (tt.nocc + tt.nvir));
+    job->t = *t;
+    job->t.range = job->range.data();
+    job->t.spin = job->spin.data();
+    job->t.sym = job->sym.data();
+    job->t.offset = job->offset.data();
+    job->t.alpha = job->alpha.empty() ? nullptr : job->alpha.data();
+    job->t.evl_sorted = job->evl.data();
+    job->f1 = *t1;
+    job->f2 = *t2;
+    job->fv = *v2;
+    job->precision = precision;
+    job->check = check_fp64 ? 1 : 0;
+    job->bytes = job_bytes(&job->t, precision);
+    if (job->bytes < 0) return fail(SDT_ERR_ARG, "sdt_server_submit: bad tiling");
+    std::lock_guard<std::mutex> lk(s->mu);
+    job->id = (int64_t)s->jobs.size();
+    job->t_submit = s->now();
+    *ticket = job->id;
+    s->queue.push_back(job.get());
+    s->jobs.push_back(std::move(job));
+    s->cv.notify_all();
+    return SDT_OK;
+}
+
+// state: 0 queued, 1 running, 2 done, -1 failed (sdt_last_error-style message
+// in msg when given).  energy: the job's (E[T], E(T)); fp64: the FP64 check
+// (when requested); times: submit, admission and completion in seconds since
+// the server was created.
+extern "C" int sdt_server_status(sdt_server *s, int64_t ticket, int *state, double *energy, double *fp64,
+                                 double *times, char *msg, size_t len) {
+    if (!s || !state) return fail(SDT_ERR_ARG, "sdt_server_status: null argument");
+    std::lock_guard<std::mutex> lk(s->mu);
+    if (ticket < 0 || ticket >= (int64_t)s->jobs.size()) return fail(SDT_ERR_ARG, "sdt_server_status: bad ticket");
+    const auto &j = *s->jobs[ticket];
+    *state = j.state;
+    if (energy) energy[0] = j.e[0], energy[1] = j.e[1];
+    if (fp64) fp64[0] = j.f[0], fp64[1] = j.f[1];
+    if (times) times[0] = j.t_submit, times[1] = j.t_start, times[2] = j.t_end;
+    if (msg && len) std::snprintf(msg, len, "%s", j.msg.c_str());
+    return j.state < 0 ? j.err : SDT_OK;
+}
+
+// Waits until every submitted job has finished (or timeout_s passed:
+// SDT_ERR_TIMEOUT).
+extern "C" int sdt_server_drain(sdt_server *s, double timeout_s) {
+    if (!s) return fail(SDT_ERR_ARG, "sdt_server_drain: null server");
+    std::unique_lock<std::mutex> lk(s->mu);
+    auto done = [&] {
+        if (!s->queue.empty() || s->adm.busy) return false;
+        return true;
+    };
+    if (!s->cv.wait_for(lk, std::chrono::duration<double>(timeout_s), done))
+        return fail(SDT_ERR_TIMEOUT, "sdt_server_drain: jobs still running");
+    return SDT_OK;
+}
+
+extern "C" int64_t sdt_server_peak_bytes(sdt_server *s) {
+    if (!s) return -1;
+    std::lock_guard<std::mutex> lk(s->mu);
+    return s->adm.peak;
+}
+
+// Stops the workers after their running jobs; queued jobs are dropped.
+extern "C" int sdt_server_destroy(sdt_server *s) {
+    if (!s) return SDT_OK;
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        s->stop = true;
+        s->cv.notify_all();
+    }
+    for (auto &w : s->workers) w.join();
+    delete s;
+    return SDT_OK;
+}
+
+// The admission policy alone, as an event simulation: n jobs arriving at
+// arrival[q] (ascending) with device bytes bytes[q] and run times
+// service[q]; start[q] and end[q] receive admission and completion times
+// (-1 for a job larger than the budget).  No GPU is used.
+extern "C" int sdt_admission_simulate(int64_t n, const double *arrival, const int64_t *bytes, const double *service,
+                                      int64_t budget, int slots, double *start, double *end) {
+    if (n < 0 || (n > 0 && (!arrival || !bytes || !service || !start || !end)) || budget <= 0 || slots < 1)
+        return fail(SDT_ERR_ARG, "sdt_admission_simulate: bad argument");
+    Admission adm;
+    adm.budget = budget;
+    adm.slots = slots;
+    std::vector<std::pair<double, int64_t>> running;  // (end time, job)
+    int64_t head = 0;
+    double clock = 0.0;
+    while (head < n || !running.empty()) {
+        // admit in FIFO order everything that has arrived and fits now
+        bool progress = true;
+        while (progress && head < n && arrival[head] <= clock) {
+            progress = false;
+            if (!adm.fits_ever(bytes[head])) {
+                start[head] = end[head] = -1.0;
+                ++head;
+                progress = true;
+            } else if (adm.can_admit(bytes[head])) {
+                adm.admit(bytes[head]);
+                start[head] = clock;
+                end[head] = clock + service[head];
+                running.emplace_back(end[head], head);
+                ++head;
+                progress = true;
+            }
+        }
+        // next event: the earliest completion or the next arrival
+        double next = 1e300;
+        for (auto &r : running) next = std::min(next, r.first);
+        if (head < n && (adm.can_admit(bytes[head]) || !adm.fits_ever(bytes[head])))
+            next = std::min(next, std::max(clock, arrival[head]));
+        if (next >= 1e300) break;
+        clock = next;
+        for (size_t q = 0; q < running.size();) {
+            if (running[q].first <= clock) {
+                adm.release(bytes[running[q].second]);
+                running[q] = running.back();
+                running.pop_back();
+            } else {
+                ++q;
+            }
+        }
+    }
+    return SDT_OK;
+}

@@ -1151,11 +1151,13 @@ int mixed_grid(sdt_job *j, int cluster, int64_t n_super, int *grid) {
             r = cuda_check(cudaOccupancyMaxActiveClusters(&ncl, kern, &cfg), "mixed form: cluster occupancy");
             if (r) return r;
             if (ncl < 1) return fail(SDT_ERR_CUDA, "mixed form: no cluster of 4 CTAs fits on this device");
+            if (j->max_ctas > 0) ncl = std::max(1, std::min(ncl, j->max_ctas / 4));
             *grid = (int)(4 * std::max<int64_t>(1, std::min<int64_t>(ncl, n_super)));
         } else {
             int nsm = 0;
             r = cuda_check(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, j->dev), "mixed form");
             if (r) return r;
+            if (j->max_ctas > 0) nsm = std::min(nsm, j->max_ctas);
             *grid = (int)std::max<int64_t>(1, std::min<int64_t>(nsm, n_super));
         }
         return SDT_OK;

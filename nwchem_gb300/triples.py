@@ -13,6 +13,7 @@ data, each block row-major in its key order.
 from __future__ import annotations
 
 import ctypes as C
+import weakref
 from dataclasses import dataclass
 
 import numpy as np
@@ -111,6 +112,7 @@ class TriplesJob:
         h = C.c_void_p()
         _capi.check(self._lib.sdt_job_create(C.byref(self._ts), C.byref(h)), "sdt_job_create")
         self._h = h
+        self._plans = weakref.WeakSet()
 
     def load(self, t1: TceFile, t2: TceFile, v2: TceFile, stream=None) -> None:
         s = [t1.struct(), t2.struct(), v2.struct()]
@@ -150,6 +152,8 @@ class TriplesJob:
 
     def close(self) -> None:
         if self._h:
+            for p in list(self._plans):  # plans are bound to the job: free them first
+                p.close()
             self._lib.sdt_job_destroy(self._h)
             self._h = C.c_void_p()
 
@@ -197,6 +201,7 @@ class Plan:
             "sdt_plan_create")
         self._h = h
         self.precision = int(precision)
+        job._plans.add(self)
 
     @property
     def items(self) -> int:

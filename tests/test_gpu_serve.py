@@ -1,0 +1,52 @@
+"""GPU tests of the serving loop: every served job's energies are the bits
+of the same job run alone; admitted jobs overlap; the byte budget holds;
+a job larger than the budget is refused; the FP64 check is the FP64 form."""
+import time
+
+import numpy as np
+import pytest
+
+import nwchem_gb300 as ng
+from nwchem_gb300 import serve
+
+pytestmark = pytest.mark.gpu
+
+
+def _alone(spec, files, prec):
+    with ng.TriplesJob(spec.tiling) as job:
+        job.load(*files)
+        kl = ng.task_list(spec.tiling)
+        return job.run(kl, precision=prec), job.run(kl)
+
+
+def test_served_jobs_match_alone_and_overlap(cuda_device):
+    specs = serve.job_stream(8, 200.0, 11, 8, 20)
+    files = serve.prepare(specs)
+    prec = ng.PREC_MIXED_FP16
+    need = [serve.job_bytes(s.tiling, prec) for s in specs]
+    budget = int(sum(sorted(need)[-3:]))              # room for about three jobs at a time
+    with serve.Server(budget, slots=3) as srv:
+        tickets = [srv.submit(s.tiling, f, prec, check_fp64=(s.id % 4 == 0)) for s, f in zip(specs, files)]
+        srv.drain(600)
+        st = [srv.status(t) for t in tickets]
+        peak = srv.peak_bytes
+    assert all(x["state"] == 2 for x in st), [x["msg"] for x in st]
+    assert peak <= budget
+    for spec, f, x in zip(specs, files, st):
+        mixed, fp64 = _alone(spec, f, prec)
+        assert x["energy"] == mixed                    # the same bits alone and in the mix
+        if spec.id % 4 == 0:
+            assert x["fp64"] == fp64
+        assert x["energy"][1] == pytest.approx(fp64[1], rel=2e-6)
+    iv = sorted((x["admitted"], x["finished"]) for x in st)
+    assert any(iv[q + 1][0] < iv[q][1] for q in range(len(iv) - 1))   # some jobs ran together
+
+
+def test_job_over_budget_is_refused(cuda_device):
+    spec = serve.job_stream(1, 10.0, 3, 16, 16)[0]
+    files = serve.prepare([spec])[0]
+    with serve.Server(1 << 20, slots=1) as srv:
+        tk = srv.submit(spec.tiling, files)
+        srv.drain(60)
+        x = srv.status(tk)
+    assert x["state"] == -1 and x["rc"] == 3 and "budget" in x["msg"]

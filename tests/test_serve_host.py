@@ -1,0 +1,73 @@
+"""CPU tests of the serving host logic: the admission policy (simulated),
+the device-byte bound used for admission, and the seeded job stream."""
+import numpy as np
+import pytest
+
+import nwchem_gb300 as ng
+from nwchem_gb300 import serve
+
+
+def _check_policy(arr, nb, svc, budget, slots):
+    start, end = serve.simulate(arr, nb, svc, budget, slots)
+    ok = start >= 0
+    assert np.array_equal(ok, nb <= budget)            # only jobs larger than the budget are refused
+    assert np.all(start[ok] >= arr[ok] - 1e-12)
+    assert np.allclose(end[ok] - start[ok], svc[ok])
+    s = start[ok]
+    assert np.all(np.diff(s) >= -1e-12)                # FIFO admission
+    # at every admission: running jobs within slots and bytes within budget
+    for q in np.flatnonzero(ok):
+        t = start[q]
+        run = ok & (start <= t + 1e-12) & (end > t + 1e-12)
+        assert run.sum() <= slots
+        assert nb[run].sum() <= budget
+    return start, end
+
+
+def test_admission_policy_random_streams():
+    rng = np.random.default_rng(0)
+    for trial in range(20):
+        n = int(rng.integers(1, 60))
+        arr = np.cumsum(rng.exponential(0.02, n))
+        nb = rng.integers(1, 100, n).astype(np.int64)
+        svc = rng.uniform(0.001, 0.2, n)
+        budget, slots = int(rng.integers(60, 200)), int(rng.integers(1, 5))
+        nb[rng.random(n) < 0.05] = budget + 1           # a few that can never fit
+        _check_policy(arr, nb, svc, budget, slots)
+
+
+def test_admission_waits_for_memory_then_starts_at_release():
+    arr = np.array([0.0, 0.0, 0.0])
+    nb = np.array([60, 60, 30], dtype=np.int64)
+    svc = np.array([1.0, 1.0, 1.0])
+    start, end = _check_policy(arr, nb, svc, 100, 4)
+    # job 1 does not fit beside job 0; FIFO keeps job 2 behind it
+    assert start.tolist() == [0.0, 1.0, 1.0] and end.tolist() == [1.0, 2.0, 2.0]
+
+
+def test_admission_is_work_conserving_when_everything_fits():
+    arr = np.linspace(0, 1, 11)
+    nb = np.ones(11, dtype=np.int64)
+    svc = np.full(11, 0.05)
+    start, _ = _check_policy(arr, nb, svc, 100, 2)
+    assert np.allclose(start, arr)
+
+
+def test_job_bytes_bound():
+    t = ng.Tiling([8, 12], [16, 24, 32]).with_evl(0)
+    f64, mx = serve.job_bytes(t, ng.PREC_FP64), serve.job_bytes(t, ng.PREC_MIXED_FP16)
+    o, v = t.nocc, t.nvir
+    assert f64 >= 8 * 3 * v * v * o * o and mx > f64
+    big = ng.Tiling([8, 12, 16], [16, 24, 32, 48]).with_evl(0)
+    assert serve.job_bytes(big, ng.PREC_MIXED_FP16) > mx
+
+
+def test_job_stream_is_seeded_and_sized():
+    a, b = serve.job_stream(30, 50.0, 7, 8, 40), serve.job_stream(30, 50.0, 7, 8, 40)
+    assert [s.arrival for s in a] == [s.arrival for s in b]
+    for s in a:
+        t = s.tiling
+        assert 8 <= t.nocc <= 40 and 5 * t.nocc - 1 <= t.nvir <= 8 * t.nocc + 1
+        assert set(t.occ[:-1]) <= set(serve.OCC_SIZES) and set(t.vir[:-1]) <= set(serve.VIR_SIZES)
+    arr = np.array([s.arrival for s in a])
+    assert np.all(np.diff(arr) > 0) and 0.2 < arr[-1] < 1.5   # ~30 jobs at 50/s
