@@ -328,7 +328,13 @@ def profile_case(args) -> None:  # noqa: C901
 
     import nwchem_gb300 as ng
     torch.cuda.set_device(0)
-    if args.case == "o64v128":
+    if args.case == "sym8s":
+        # blocked symmetry, small: o=48 as 6x8 (irreps 0..5), v=128 as 8x16 (irreps 0..7), seed 3
+        t = ng.Tiling([8] * 6, [16] * 8, occ_sym=list(range(6)), vir_sym=list(range(8)), name="sym8s").with_evl(3)
+        files = ng.synth_inputs(t, 3)
+        kl = ng.task_list(t)
+        sel = kl[:args.tuples]
+    elif args.case == "o64v128":
         # whole 8x8x8x4x4x4 sub-boxes, as in the o=64/v=512 workload
         t = ng.Tiling([32, 32], [64, 64], name="o64v128").with_evl(2)
         files = ng.synth_inputs(t, 2)
@@ -532,7 +538,7 @@ def main() -> None:
     ap.add_argument("--omax", type=int, default=24, help="serve: largest occupied size")
     ap.add_argument("--slots", type=int, default=4, help="serve: worker slots")
     ap.add_argument("--max-ctas", type=int, default=0, help="serve: CTA cap per job launch (0: all SMs)")
-    ap.add_argument("--case", default="o40v114", choices=["o40v114", "o64v128"], help="--profile case")
+    ap.add_argument("--case", default="o40v114", choices=["o40v114", "o64v128", "sym8s"], help="--profile case")
     ap.add_argument("--kseg", type=int, default=0, help="mixed form: K chunks per accumulator drain")
     ap.add_argument("--mixed", default="", choices=["", "tf32", "bf16", "fp16"],
                     help="--profile case in a mixed form")
