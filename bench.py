@@ -349,10 +349,12 @@ def profile_case(args) -> None:  # noqa: C901
     with ng.TriplesJob(t) as job:
         job.load(*files)
         job.set_timing(True)
+        job.set_mixed_cluster(args.shape)
         prec = dict(MIXED_FORMS).get(args.mixed, ng.PREC_FP64)
         job.run(sel, precision=prec)
         e = job.run(sel, precision=prec)
-        print(json.dumps({"profile_case": args.case, "form": args.mixed or "fp64", "tuples": int(len(sel)),
+        print(json.dumps({"profile_case": args.case, "form": args.mixed or "fp64", "shape": args.shape,
+                          "tuples": int(len(sel)),
                           "flops": ng.flops(t, sel),
                           "kernel_ms": job.last_kernel_ms, "device_bytes": job.device_bytes,
                           "tflops": ng.flops(t, sel) / job.last_kernel_ms / 1e9, "energies": list(e)}),
@@ -539,6 +541,7 @@ def main() -> None:
     ap.add_argument("--slots", type=int, default=4, help="serve: worker slots")
     ap.add_argument("--max-ctas", type=int, default=0, help="serve: CTA cap per job launch (0: all SMs)")
     ap.add_argument("--case", default="o40v114", choices=["o40v114", "o64v128", "sym8s"], help="--profile case")
+    ap.add_argument("--shape", type=int, default=1, choices=[1, 2, 4], help="mixed work-unit shape")
     ap.add_argument("--kseg", type=int, default=0, help="mixed form: K chunks per accumulator drain")
     ap.add_argument("--mixed", default="", choices=["", "tf32", "bf16", "fp16"],
                     help="--profile case in a mixed form")

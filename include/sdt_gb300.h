@@ -228,9 +228,13 @@ int64_t sdt_job_device_bytes(const sdt_job *job);
  * chains reduce the FP32 rounding of the split products at the cost of more
  * drains. */
 int sdt_job_set_mixed_segment(sdt_job *job, int chunks);
-/* Mixed form: run the kernel in clusters of `ctas` CTAs (1, the default, or
- * 4).  With 4, the CTAs of a cluster take sub-boxes that differ in the j and
- * k boxes and multicast the operand tiles they share. */
+/* Mixed form: the kernel's work-unit shape.  1 (the default): one CTA per
+ * sub-box, the finished sub-box kept in registers while the next one is
+ * contracted; 2: the same with the finished sub-box kept in tensor memory
+ * (one accumulator instead of two, the energy work gets the registers --
+ * for tuples whose spin/irrep-kept K is short); 4: clusters of 4 CTAs whose
+ * sub-boxes differ in the j and k boxes and that multicast the operand
+ * tiles they share. */
 int sdt_job_set_mixed_cluster(sdt_job *job, int ctas);
 /* When on, sdt_job_run brackets its fused-kernel launches with CUDA events
  * on the run's stream; sdt_job_last_kernel_ms returns that interval. */
@@ -241,8 +245,8 @@ double sdt_job_last_kernel_ms(const sdt_job *job);
  * list.  sdt_plan_create checks the list, builds the work indexes, sizes
  * the persistent launches (and, for a mixed precision, encodes the job's
  * split operands if needed) and uploads them; ctas (optional, one per
- * tuple, 1 or 4) picks the mixed kernel's work-unit shape per tuple (4: a
- * cluster of 4 CTAs takes a 2x2 tile of (j,k) sub-boxes).
+ * tuple: 1, 2 or 4 as in sdt_job_set_mixed_cluster) picks the mixed
+ * kernel's work-unit shape per tuple.
  * sdt_plan_launch only enqueues device work -- per group a queue reset and
  * one persistent kernel, the compensated sums and the copy of the results
  * to pinned host memory -- and can be recorded by stream capture;

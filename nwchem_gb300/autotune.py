@@ -4,8 +4,11 @@ The reference schedules tuples by weight only (ccsd_t_neword.F); on GB300
 the batched path also chooses, per job, which split encoding runs the d1/d2
 contractions (TF32x3, BF16x3 or scaled FP16x3, among the forms the caller's
 accuracy allows) and, per size class of tuples, the kernel's work-unit
-shape: one 8x8x8x4x4x4 sub-box per CTA, or a 2x2 tile of (j,k) sub-boxes per
-cluster of 4 CTAs that multicast the operand tiles they share.
+shape: one 8x8x8x4x4x4 sub-box per CTA with the finished sub-box held in
+registers (two tensor-memory accumulators), the same with it held in tensor
+memory (one accumulator, free registers for the FP64 energy work), or a 2x2
+tile of (j,k) sub-boxes per cluster of 4 CTAs that multicast the operand
+tiles they share.
 
 A size class is the pair (log2 of the tuple's virtual sub-box count,
 log2 of its occupied sub-box count), rounded.  For each class the tuner
@@ -29,7 +32,7 @@ from .tiling import Tiling
 from .triples import PREC_MIXED_BF16, PREC_MIXED_FP16, PREC_MIXED_TF32, Plan, TriplesJob, flops
 
 FORMS = {"tf32": PREC_MIXED_TF32, "bf16": PREC_MIXED_BF16, "fp16": PREC_MIXED_FP16}
-SHAPES = (1, 4)  # CTAs per work unit
+SHAPES = (1, 2, 4)  # work-unit shapes: 1 CTA, 1 CTA with the sub-box kept in TMEM, cluster of 4
 
 Measure = Callable[[np.ndarray, int, int], float]
 

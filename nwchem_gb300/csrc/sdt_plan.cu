@@ -66,7 +66,9 @@ int mixed_type_of(int precision) {
     return precision == SDT_PREC_MIXED_TF32 ? TM_F32 : precision == SDT_PREC_MIXED_BF16 ? TM_BF16 : TM_F16;
 }
 
-// Builds a plan; ctas[q] (optional, caller order) is the cluster size of tuple q.
+// Builds a plan; ctas[q] (optional, caller order) is the work-unit shape of
+// tuple q: 1 one CTA per sub-box, 2 the same with the finished sub-box kept in
+// tensor memory, 4 clusters of 4 CTAs on 2x2 (j,k) sub-box tiles.
 int plan_create(sdt_job *j, const int64_t *klist, int64_t n, int precision, const int32_t *ctas,
                 sdt_plan **out, const char *who) {
     *out = nullptr;
@@ -86,8 +88,8 @@ int plan_create(sdt_job *j, const int64_t *klist, int64_t n, int precision, cons
         }
         if (!(k[0] <= k[1] && k[1] <= k[2] && k[3] <= k[4] && k[4] <= k[5]))
             return fail(SDT_ERR_ARG, std::string(who) + ": tuple tiles not sorted");
-        if (ctas && ctas[q] != 1 && ctas[q] != 4)
-            return fail(SDT_ERR_ARG, std::string(who) + ": cluster size must be 1 or 4");
+        if (ctas && ctas[q] != 1 && ctas[q] != 2 && ctas[q] != 4)
+            return fail(SDT_ERR_ARG, std::string(who) + ": work-unit shape must be 1, 2 or 4");
     }
     sdt_plan *p = new sdt_plan();
     p->job = j;
@@ -95,7 +97,7 @@ int plan_create(sdt_job *j, const int64_t *klist, int64_t n, int precision, cons
     p->n = n;
     // Group by cluster size (FP64: one group), keeping the caller's order inside a group.
     auto cl = [&](int64_t q) { return mixed ? (ctas ? (int)ctas[q] : j->mixed_cluster) : 1; };
-    for (int c : {1, 4})
+    for (int c : {1, 2, 4})
         for (int64_t q = 0; q < n; ++q)
             if (cl(q) == c) p->order.push_back(q);
     const int box_v = mixed ? 8 : 4, box_o = 4;

@@ -115,6 +115,7 @@ __device__ __forceinline__ int xaddr(int a, int b, int c, int i, int j, int k) {
 struct EDesc {
     int g[6];       // global orbital index of the sub-box origin, per dimension
     int nv[6];      // valid extent of the sub-box, per dimension
+    int gp[6];      // holes (3..5): padded hole index of the origin (FP32 s1 copies)
     double factor;  // the tuple's multiplicity factor
     long long item;
 };
@@ -135,7 +136,8 @@ struct SplitParams {
     const uint8_t *blk[2 * L_N];  // [2*layout + (0 hi, 1 lo)]
     const int32_t *tile_box;      // [ntiles]: global box id of the tile's first box (its space)
     const int64_t *pair_blk;      // [nvab*nvab]: first Vd2 block of tile pair (B<=C), -1 none
-    const float *T1f, *Uf;        // FP32 copies: [v][o], [v][v][o][o]
+    const float *T1f, *Uf;        // FP32 copies: [v][OP], [v][v][OP][OP], holes padded per tile to 4
+    int32_t op;                   // OP, the padded hole count (4 x hole boxes)
     const double *evl;
     const int32_t *tiles;         // [ntiles][4] start, range, spin, sym
     int32_t noab, nvab, nk_o, nk_v, kseg, nob, nvb;
@@ -406,7 +408,7 @@ __device__ __forceinline__ void run_producer(const SplitParams &p, uint8_t *stag
 
 // ---------------------------------------------------------------------------
 // MMA issuer (one thread).
-template <int TYPE, int CS>
+template <int TYPE, int CS, int NB>
 __device__ __forceinline__ void run_mma(const SplitParams &p, uint8_t *stages, uint64_t *full, uint64_t *empty,
                                         uint64_t *tfull, uint64_t *tempty, uint64_t *drain, uint32_t tmem,
                                         volatile int *abort, int rj, int rk, int64_t unit0, int64_t ustep,
@@ -432,8 +434,8 @@ __device__ __forceinline__ void run_mma(const SplitParams &p, uint8_t *stages, u
             int kseg;
             const int nseg = term_segments(nk, p.kseg, kseg);
             for (int sgi = 0; sgi < nseg && !stop; ++sgi, ++sg) {
-                const int buf = sg & 1;
-                if (sg >= 2 && !tc::mbar_wait(&tempty[buf], ((sg >> 1) - 1) & 1, kWaitNs, abort)) {
+                const int buf = sg % NB;  // NB accumulators of 256 columns
+                if (sg >= NB && !tc::mbar_wait(&tempty[buf], ((sg / NB) - 1) & 1, kWaitNs, abort)) {
                     stop = true;
                     break;
                 }
@@ -502,6 +504,21 @@ __device__ __forceinline__ void drain_term(float *X, uint32_t taddr, int m) {
     }
 }
 
+// The last term's drain when the sub-box is kept in tensor memory: the sum
+// of the sub-box value and the accumulator goes to the hold region (row m =
+// (b;i,j), column 32a + 4c + k), not back to shared memory.
+__device__ __forceinline__ void drain_hold(const float *X, uint32_t tacc, uint32_t thold, int m) {
+    const int b = m >> 4, i = (m >> 2) & 3, j = m & 3;
+#pragma unroll 1
+    for (int cc = 0; cc < 8; ++cc) {
+        float v[32], w[32];
+        tc::tmem_ld32(tacc + (uint32_t)(cc * 32), v);
+#pragma unroll
+        for (int q = 0; q < 32; ++q) w[q] = X[xaddr(cc, b, q >> 2, i, j, q & 3)] + v[q];  // term 8: sign +1
+        tc::tmem_st32(thold + (uint32_t)(cc * 32), w);
+    }
+}
+
 __device__ __forceinline__ void drain_any(int t, bool store, float *X, uint32_t taddr, int m) {
     switch (t) {
         case 0:
@@ -542,14 +559,21 @@ __device__ __forceinline__ double widen(float f) {
 //       + t1(c,i)u(a,b,j,k) - t1(c,j)u(a,b,i,k) + t1(c,k)u(a,b,i,j)   (FP32)
 //   D = (e_i + e_j + e_k) - (e_a + e_b + e_c)                          (FP64)
 //   e1 += X^2 / D,  est += X X_s / D                                    (FP64)
-template <int A>
-__device__ __forceinline__ void energy_chunk(const float (&R)[128], const EDesc &d, const SplitParams &p, int half,
+__device__ __forceinline__ float4 ld4(const float *p) { return __ldg(reinterpret_cast<const float4 *>(p)); }
+__device__ __forceinline__ float el(const float4 &x, int k) { return k == 0 ? x.x : k == 1 ? x.y : k == 2 ? x.z : x.w; }
+
+// The s1 operands are FP32 copies with every occupied tile padded to a
+// multiple of 4 holes, so the 4 k values of a sub-box are one aligned float4.
+// R[OFF + 4*c + k] holds local (a = 4*half + A, b, c, i, j, k).
+template <int A, int OFF, int N>
+__device__ __forceinline__ void energy_chunk(const float (&R)[N], const EDesc &d, const SplitParams &p, int half,
                                              int b, int i, int j, double &e1, double &est) {
     const int a = 4 * half + A;
     if (a >= d.nv[0] || b >= d.nv[1] || i >= d.nv[3] || j >= d.nv[4]) return;
-    const int o = (int)p.nocc;
-    const int64_t v = p.nvir, oo = (int64_t)o * o;
+    const int op = p.op;
+    const int64_t v = p.nvir, oo = (int64_t)op * op;
     const int ga = d.g[0] + a, gb = d.g[1] + b, gi = d.g[3] + i, gj = d.g[4] + j;
+    const int pi = d.gp[3] + i, pj = d.gp[4] + j, pk0 = d.gp[5];  // padded holes
     const int nc = d.nv[2], nk = d.nv[5], gc0 = d.g[2], gk0 = d.g[5];
     const double *__restrict__ eo = p.evl;
     const double *__restrict__ ev = p.evl + p.nocc;
@@ -558,35 +582,116 @@ __device__ __forceinline__ void energy_chunk(const float (&R)[128], const EDesc 
     double P[4];  // e_i + e_j + e_k
 #pragma unroll
     for (int k = 0; k < 4; ++k) P[k] = k < nk ? eij + __ldg(eo + gk0 + k) : 0.0;
-    const float *__restrict__ t1a = p.T1f + (int64_t)ga * o;
-    const float *__restrict__ t1b = p.T1f + (int64_t)gb * o;
-    const float t1ai = __ldg(t1a + gi), t1aj = __ldg(t1a + gj), t1bi = __ldg(t1b + gi), t1bj = __ldg(t1b + gj);
+    const float *__restrict__ t1a = p.T1f + (int64_t)ga * op;
+    const float *__restrict__ t1b = p.T1f + (int64_t)gb * op;
+    const float t1ai = __ldg(t1a + pi), t1aj = __ldg(t1a + pj), t1bi = __ldg(t1b + pi), t1bj = __ldg(t1b + pj);
+    const float4 t1ak = ld4(t1a + pk0), t1bk = ld4(t1b + pk0);
     const float *__restrict__ uab = p.Uf + ((int64_t)ga * v + gb) * oo;
-    const float uabij = __ldg(uab + gi * o + gj);
+    const float uabij = __ldg(uab + pi * op + pj);
+    const float4 uabj = ld4(uab + pj * op + pk0), uabi = ld4(uab + pi * op + pk0);
 #pragma unroll
     for (int c = 0; c < 8; ++c) {
         if (c < nc) {
             const int gc = gc0 + c;
-            const float *__restrict__ t1c = p.T1f + (int64_t)gc * o;
+            const float *__restrict__ t1c = p.T1f + (int64_t)gc * op;
             const float *__restrict__ ubc = p.Uf + ((int64_t)gb * v + gc) * oo;
             const float *__restrict__ uac = p.Uf + ((int64_t)ga * v + gc) * oo;
-            const float t1ci = __ldg(t1c + gi), t1cj = __ldg(t1c + gj);
-            const float ubcij = __ldg(ubc + gi * o + gj), uacij = __ldg(uac + gi * o + gj);
+            const float t1ci = __ldg(t1c + pi), t1cj = __ldg(t1c + pj);
+            const float ubcij = __ldg(ubc + pi * op + pj), uacij = __ldg(uac + pi * op + pj);
+            const float4 ubcj = ld4(ubc + pj * op + pk0), ubci = ld4(ubc + pi * op + pk0);
+            const float4 uacj = ld4(uac + pj * op + pk0), uaci = ld4(uac + pi * op + pk0);
+            const float4 t1ck = ld4(t1c + pk0);
             const double Q = eab + __ldg(ev + gc);
 #pragma unroll
             for (int k = 0; k < 4; ++k) {
                 if (k < nk) {
-                    const int gk = gk0 + k;
-                    float s = t1ai * __ldg(ubc + gj * o + gk);
-                    s = fmaf(-t1aj, __ldg(ubc + gi * o + gk), s);
-                    s = fmaf(__ldg(t1a + gk), ubcij, s);
-                    s = fmaf(-t1bi, __ldg(uac + gj * o + gk), s);
-                    s = fmaf(t1bj, __ldg(uac + gi * o + gk), s);
-                    s = fmaf(-__ldg(t1b + gk), uacij, s);
-                    s = fmaf(t1ci, __ldg(uab + gj * o + gk), s);
-                    s = fmaf(-t1cj, __ldg(uab + gi * o + gk), s);
-                    s = fmaf(__ldg(t1c + gk), uabij, s);
-                    const double x = widen(R[A * 32 + c * 4 + k]);
+                    float s = t1ai * el(ubcj, k);
+                    s = fmaf(-t1aj, el(ubci, k), s);
+                    s = fmaf(el(t1ak, k), ubcij, s);
+                    s = fmaf(-t1bi, el(uacj, k), s);
+                    s = fmaf(t1bj, el(uaci, k), s);
+                    s = fmaf(-el(t1bk, k), uacij, s);
+                    s = fmaf(t1ci, el(uabj, k), s);
+                    s = fmaf(-t1cj, el(uabi, k), s);
+                    s = fmaf(el(t1ck, k), uabij, s);
+                    const double x = widen(R[OFF + c * 4 + k]);
+                    const double D = P[k] - Q;
+                    const double q = div_nr(x, D);
+                    e1 = fma(q, x, e1);
+                    est = fma(q, widen(s), est);
+                }
+            }
+        }
+    }
+}
+
+// The same energies reading the finished sub-box from the tensor-memory hold
+// columns (th: this warp's lane quadrant, column 128*half), 4 columns (the
+// k values of one c) at a time in rolled loops: a small loop body, and
+// registers free for the FP64 work.  All lanes take part in every TMEM load.
+__device__ __forceinline__ void energy_tmem(uint32_t th, const EDesc &d, const SplitParams &p, int half, int b,
+                                            int i, int j, double &e1, double &est) {
+    const bool row_ok = b < d.nv[1] && i < d.nv[3] && j < d.nv[4];
+    const int op = p.op;
+    const int64_t v = p.nvir, oo = (int64_t)op * op;
+    const int gb = d.g[1] + b, gi = d.g[3] + i, gj = d.g[4] + j;
+    const int pi = d.gp[3] + i, pj = d.gp[4] + j, pk0 = d.gp[5];
+    const int nc = d.nv[2], nk = d.nv[5], gc0 = d.g[2], gk0 = d.g[5];
+    const double *__restrict__ eo = p.evl;
+    const double *__restrict__ ev = p.evl + p.nocc;
+    double P[4];
+    const double eij = row_ok ? __ldg(eo + gi) + __ldg(eo + gj) : 0.0;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) P[k] = (row_ok && k < nk) ? eij + __ldg(eo + gk0 + k) : 0.0;
+    const float *__restrict__ t1b = p.T1f + (int64_t)(row_ok ? gb : 0) * op;
+    const float t1bi = row_ok ? __ldg(t1b + pi) : 0.f, t1bj = row_ok ? __ldg(t1b + pj) : 0.f;
+    const float4 t1bk = row_ok ? ld4(t1b + pk0) : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll 1
+    for (int A = 0; A < 4; ++A) {
+        const int a = 4 * half + A;
+        const bool ok_a = row_ok && a < d.nv[0];
+        const int ga = d.g[0] + a;
+        const float *__restrict__ t1a = p.T1f + (int64_t)(ok_a ? ga : 0) * op;
+        const float *__restrict__ uab = p.Uf + ((int64_t)(ok_a ? ga : 0) * v + (ok_a ? gb : 0)) * oo;
+        float t1ai = 0.f, t1aj = 0.f, uabij = 0.f;
+        float4 t1ak = make_float4(0.f, 0.f, 0.f, 0.f), uabj = t1ak, uabi = t1ak;
+        double eab = 0.0;
+        if (ok_a) {
+            t1ai = __ldg(t1a + pi);
+            t1aj = __ldg(t1a + pj);
+            t1ak = ld4(t1a + pk0);
+            uabij = __ldg(uab + pi * op + pj);
+            uabj = ld4(uab + pj * op + pk0);
+            uabi = ld4(uab + pi * op + pk0);
+            eab = __ldg(ev + ga) + __ldg(ev + gb);
+        }
+#pragma unroll 1
+        for (int c = 0; c < 8; ++c) {
+            const float4 x4 = tc::tmem_ld4(th + (uint32_t)(32 * A + 4 * c));  // every lane
+            if (!ok_a || c >= nc) continue;
+            const int gc = gc0 + c;
+            const float *__restrict__ t1c = p.T1f + (int64_t)gc * op;
+            const float *__restrict__ ubc = p.Uf + ((int64_t)gb * v + gc) * oo;
+            const float *__restrict__ uac = p.Uf + ((int64_t)ga * v + gc) * oo;
+            const float t1ci = __ldg(t1c + pi), t1cj = __ldg(t1c + pj);
+            const float ubcij = __ldg(ubc + pi * op + pj), uacij = __ldg(uac + pi * op + pj);
+            const float4 ubcj = ld4(ubc + pj * op + pk0), ubci = ld4(ubc + pi * op + pk0);
+            const float4 uacj = ld4(uac + pj * op + pk0), uaci = ld4(uac + pi * op + pk0);
+            const float4 t1ck = ld4(t1c + pk0);
+            const double Q = eab + __ldg(ev + gc);
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                if (k < nk) {
+                    float s = t1ai * el(ubcj, k);
+                    s = fmaf(-t1aj, el(ubci, k), s);
+                    s = fmaf(el(t1ak, k), ubcij, s);
+                    s = fmaf(-t1bi, el(uacj, k), s);
+                    s = fmaf(t1bj, el(uaci, k), s);
+                    s = fmaf(-el(t1bk, k), uacij, s);
+                    s = fmaf(t1ci, el(uabj, k), s);
+                    s = fmaf(-t1cj, el(uabi, k), s);
+                    s = fmaf(el(t1ck, k), uabij, s);
+                    const double x = widen(el(x4, k));
                     const double D = P[k] - Q;
                     const double q = div_nr(x, D);
                     e1 = fma(q, x, e1);
@@ -620,9 +725,15 @@ __device__ __forceinline__ void write_partial(double &e1, double &est, double *r
     est = 0.0;
 }
 
-template <int TYPE, int CS>
+// HOLD = 0: the energy warps keep the finished sub-box in registers, two
+// TMEM accumulators; HOLD = 1: the last drain writes it to the upper 256
+// TMEM columns, which the energy warps read 32 columns at a time (their
+// registers stay free for the FP64 work), one accumulator.
+template <int TYPE, int CS, int HOLD>
 __global__ void __launch_bounds__(SX_THREADS, 1) split_fused_kernel(const __grid_constant__ SplitParams p) {
+    static_assert(HOLD == 0 || CS == 1, "tensor-memory hold with single CTAs only");
     constexpr int PJ = CS == 4 ? 2 : 1;
+    constexpr int NB = HOLD ? 1 : 2;
     extern __shared__ __align__(1024) uint8_t smem_raw[];
     uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     float *X = (float *)smem;
@@ -683,7 +794,8 @@ __global__ void __launch_bounds__(SX_THREADS, 1) split_fused_kernel(const __grid
         if (warp == 0 && lane == 0)
             run_producer<TYPE, CS>(p, stages, full, empty, abort, rj, rk, unit0, ustep, ring);
         else if (warp == 1 && lane == 0)
-            run_mma<TYPE, CS>(p, stages, full, empty, tfull, tempty, drain, tmem, abort, rj, rk, unit0, ustep, ring);
+            run_mma<TYPE, CS, NB>(p, stages, full, empty, tfull, tempty, drain, tmem, abort, rj, rk, unit0, ustep,
+                                  ring);
     } else if (warp < 8) {
         // ---------------- drain warps ----------------
         asm volatile("setmaxnreg.dec.sync.aligned.u32 %0;" ::"n"(SX_REG_DRAIN));
@@ -715,12 +827,14 @@ __global__ void __launch_bounds__(SX_THREADS, 1) split_fused_kernel(const __grid
                 int kseg;
                 const int nseg = term_segments(nk, p.kseg, kseg);
                 for (int sgi = 0; sgi < nseg; ++sgi, ++sg) {
-                    const int buf = sg & 1;
+                    const int buf = sg % NB;
                     const bool first = (t == 0 && sgi == 0);
+                    const bool last = (t == 8 && sgi == nseg - 1);
                     if (leader) {
-                        bool w = tc::mbar_wait(&tfull[buf], (sg >> 1) & 1, kWaitNs, abort);
-                        // the previous item's values must have left the sub-box
-                        if (w && first && n > 0) w = tc::mbar_wait(xfree, (n - 1) & 1, kWaitNs, abort);
+                        bool w = tc::mbar_wait(&tfull[buf], (sg / NB) & 1, kWaitNs, abort);
+                        // registers hold: the previous item's values must have left the sub-box;
+                        // tensor-memory hold: they must have left the hold columns
+                        if (w && n > 0 && (HOLD ? last : first)) w = tc::mbar_wait(xfree, (n - 1) & 1, kWaitNs, abort);
                         *dr_ok = w ? 1 : 0;
                     }
                     named_bar(1, SX_DRAIN);
@@ -729,7 +843,21 @@ __global__ void __launch_bounds__(SX_THREADS, 1) split_fused_kernel(const __grid
                         break;
                     }
                     tc::tc_fence_after();
-                    if (nk > 0) {
+                    if (HOLD && last) {
+                        if (nk > 0) {
+                            drain_hold(X, tq + (uint32_t)(buf * 256), tq + 256u, m);
+                        } else {  // no kept K chunk in the last term: the sub-box as it is
+                            float z[32];
+#pragma unroll
+                            for (int q = 0; q < 32; ++q) z[q] = 0.0f;
+                            const int bb = m >> 4, ii = (m >> 2) & 3, jj = m & 3;
+                            for (int cc = 0; cc < 8; ++cc) {
+#pragma unroll
+                                for (int q = 0; q < 32; ++q) z[q] = X[xaddr(cc, bb, q >> 2, ii, jj, q & 3)];
+                                tc::tmem_st32(tq + 256u + (uint32_t)(cc * 32), z);
+                            }
+                        }
+                    } else if (nk > 0) {
                         drain_any(t, first, X, tq + (uint32_t)(buf * 256), m);
                     } else if (first) {  // no kept K chunk in the first term: start from zero
                         for (int e = m * 256; e < m * 256 + 256; ++e) X[e] = 0.0f;
@@ -755,7 +883,7 @@ __global__ void __launch_bounds__(SX_THREADS, 1) split_fused_kernel(const __grid
         const int rb = mm >> 4, ri = (mm >> 2) & 3, rj_ = mm & 3;  // thread row (b;i,j)
         const int ew = et >> 5;
         const bool leader = (et == 0);
-        float R[128];
+        float R[HOLD ? 1 : 128];
         double e1 = 0.0, est = 0.0;
         for (int n = 0;; ++n) {
             if (leader) {
@@ -771,6 +899,7 @@ __global__ void __launch_bounds__(SX_THREADS, 1) split_fused_kernel(const __grid
                         for (int dd = 0; dd < 6; ++dd) {
                             desc->g[dd] = bx.start[dd] + bx.boff[dd];
                             desc->nv[dd] = min(dd < 3 ? SX_BV : SX_BO, bx.ext[dd] - bx.boff[dd]);
+                            desc->gp[dd] = dd < 3 ? 0 : 4 * __ldg(p.tile_box + bx.tile[dd] - 1) + bx.boff[dd];
                         }
                         desc->factor = p.factor[bx.tq];
                         desc->item = bx.item;
@@ -785,21 +914,32 @@ __global__ void __launch_bounds__(SX_THREADS, 1) split_fused_kernel(const __grid
             }
             named_bar(2, SX_EPI);
             if (*en_unit < 0) break;
-#pragma unroll
-            for (int A = 0; A < 4; ++A)
-#pragma unroll
-                for (int c = 0; c < 8; ++c)
-#pragma unroll
-                    for (int k = 0; k < 4; ++k) R[A * 32 + c * 4 + k] = X[xaddr(4 * half + A, rb, c, ri, rj_, k)];
-            named_bar(2, SX_EPI);
-            if (leader) tc::mbar_arrive(xfree);
             const EDesc &d = *desc;
-            if (d.item >= 0) {  // a box outside the tuple has no item
-                energy_chunk<0>(R, d, p, half, rb, ri, rj_, e1, est);
-                energy_chunk<1>(R, d, p, half, rb, ri, rj_, e1, est);
-                energy_chunk<2>(R, d, p, half, rb, ri, rj_, e1, est);
-                energy_chunk<3>(R, d, p, half, rb, ri, rj_, e1, est);
-                write_partial(e1, est, red, d, p, ew, lane, leader);
+            if constexpr (HOLD) {
+                // the sub-box is in the hold columns: this warp's lane quadrant, columns 128*half + 32*A
+                tc::tc_fence_after();
+                const uint32_t th = tmem + ((uint32_t)((warp & 3) * 32) << 16) + 256u + (uint32_t)(128 * half);
+                if (d.item >= 0) energy_tmem(th, d, p, half, rb, ri, rj_, e1, est);
+                tc::tc_fence_before();
+                named_bar(2, SX_EPI);
+                if (leader) tc::mbar_arrive(xfree);  // the hold columns are free
+                if (d.item >= 0) write_partial(e1, est, red, d, p, ew, lane, leader);
+            } else {
+#pragma unroll
+                for (int A = 0; A < 4; ++A)
+#pragma unroll
+                    for (int c = 0; c < 8; ++c)
+#pragma unroll
+                        for (int k = 0; k < 4; ++k) R[A * 32 + c * 4 + k] = X[xaddr(4 * half + A, rb, c, ri, rj_, k)];
+                named_bar(2, SX_EPI);
+                if (leader) tc::mbar_arrive(xfree);
+                if (d.item >= 0) {  // a box outside the tuple has no item
+                    energy_chunk<0, 0, 128>(R, d, p, half, rb, ri, rj_, e1, est);
+                    energy_chunk<1, 32, 128>(R, d, p, half, rb, ri, rj_, e1, est);
+                    energy_chunk<2, 64, 128>(R, d, p, half, rb, ri, rj_, e1, est);
+                    energy_chunk<3, 96, 128>(R, d, p, half, rb, ri, rj_, e1, est);
+                    write_partial(e1, est, red, d, p, ew, lane, leader);
+                }
             }
         }
     }
@@ -913,10 +1053,32 @@ __global__ void __launch_bounds__(256) pack_blocks_kernel(const PackArgs g) {
     }
 }
 
-__global__ void __launch_bounds__(256) to_f32_kernel(const double *__restrict__ src, float *__restrict__ dst,
-                                                     int64_t n) {
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-        dst[i] = __double2float_rn(src[i]);
+// FP32 copy of rows of hole-indexed FP64 data with the trailing `nh` hole
+// indices padded per tile (padded index = 4 x box id + local; padding 0):
+// T1 [v][o] -> [v][OP] (nh = 1), the vvoo block [v][v][o][o] -> [v][v][OP][OP] (nh = 2).
+__global__ void __launch_bounds__(256) pad_f32_kernel(const double *__restrict__ src, float *__restrict__ dst,
+                                                      int64_t rows, int64_t o, int64_t op, int nh,
+                                                      const int32_t *__restrict__ orow0,
+                                                      const int32_t *__restrict__ on) {
+    const int64_t per = nh == 1 ? op : op * op;
+    const int64_t total = rows * per;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t r = i / per, rem = i % per;
+        const int64_t hk = nh == 1 ? rem : rem % op, hj = nh == 1 ? 0 : rem / op;
+        const int bk = (int)(hk >> 2), bj = (int)(hj >> 2);
+        float x = 0.0f;
+        if ((hk & 3) < on[bk] && (nh == 1 || (hj & 3) < on[bj])) {
+            const int64_t k = orow0[bk] + (hk & 3);
+            if (nh == 1) {
+                x = __double2float_rn(src[r * o + k]);
+            } else {
+                const int64_t jj = orow0[bj] + (hj & 3);
+                x = __double2float_rn(src[(r * o + jj) * o + k]);
+            }
+        }
+        dst[i] = x;
+    }
 }
 
 // max |src| as the bit pattern of a non-negative double (orders like the value).
@@ -1106,8 +1268,10 @@ int mixed_prepare(sdt_job *j, int type, cudaStream_t st) {
         else pack_blocks_kernel<TM_F16><<<gb, 256, 0, st>>>(g);
         count_launch();
     }
-    // FP32 copies of T1 [v][o] and the vvoo block [v][v][o][o] for the s1 terms.
-    const int64_t n_t1 = v * o, n_u = (int64_t)j->arr_n[DST_UD];
+    // FP32 copies of T1 [v][OP] and the vvoo block [v][v][OP][OP] for the s1
+    // terms, holes padded per tile to multiples of 4.
+    const int64_t OP = 4 * NOB;
+    const int64_t n_t1 = v * OP, n_u = v * v * OP * OP;
     if (!rc) {
         j->t1f = (float *)gpu_get(std::max<int64_t>(n_t1, 1) * sizeof(float));
         j->uf = (float *)gpu_get(std::max<int64_t>(n_u, 1) * sizeof(float));
@@ -1115,9 +1279,12 @@ int mixed_prepare(sdt_job *j, int type, cudaStream_t st) {
             mixed_release(j);
             return fail(SDT_ERR_NOMEM, "mixed form: FP32 copies");
         }
-        to_f32_kernel<<<grid_for(n_t1), 256, 0, st>>>(j->arr[DST_T1], j->t1f, n_t1);
+        const int32_t *t32 = (const int32_t *)tab_d;
+        pad_f32_kernel<<<grid_for(n_t1), 256, 0, st>>>(j->arr[DST_T1], j->t1f, v, o, OP, 1, t32 + 2 * o_orow0,
+                                                       t32 + 2 * o_on);
         count_launch();
-        to_f32_kernel<<<grid_for(n_u), 256, 0, st>>>(j->arr[DST_UD], j->uf, n_u);
+        pad_f32_kernel<<<grid_for(n_u), 256, 0, st>>>(j->arr[DST_UD], j->uf, v * v, o, OP, 2, t32 + 2 * o_orow0,
+                                                      t32 + 2 * o_on);
         count_launch();
         rc = cuda_check(cudaGetLastError(), "mixed form: split");
     }
@@ -1164,13 +1331,18 @@ int mixed_grid(sdt_job *j, int cluster, int64_t n_super, int *grid) {
     };
     const int type = j->mixed_type;
     if (cluster == 4) {
-        if (type == TM_F32) return setup(split_fused_kernel<TM_F32, 4>);
-        if (type == TM_BF16) return setup(split_fused_kernel<TM_BF16, 4>);
-        return setup(split_fused_kernel<TM_F16, 4>);
+        if (type == TM_F32) return setup(split_fused_kernel<TM_F32, 4, 0>);
+        if (type == TM_BF16) return setup(split_fused_kernel<TM_BF16, 4, 0>);
+        return setup(split_fused_kernel<TM_F16, 4, 0>);
     }
-    if (type == TM_F32) return setup(split_fused_kernel<TM_F32, 1>);
-    if (type == TM_BF16) return setup(split_fused_kernel<TM_BF16, 1>);
-    return setup(split_fused_kernel<TM_F16, 1>);
+    if (cluster == 2) {
+        if (type == TM_F32) return setup(split_fused_kernel<TM_F32, 1, 1>);
+        if (type == TM_BF16) return setup(split_fused_kernel<TM_BF16, 1, 1>);
+        return setup(split_fused_kernel<TM_F16, 1, 1>);
+    }
+    if (type == TM_F32) return setup(split_fused_kernel<TM_F32, 1, 0>);
+    if (type == TM_BF16) return setup(split_fused_kernel<TM_BF16, 1, 0>);
+    return setup(split_fused_kernel<TM_F16, 1, 0>);
 }
 
 int mixed_launch(sdt_job *j, const LaunchArgs &a, cudaStream_t st) {
@@ -1183,6 +1355,7 @@ int mixed_launch(sdt_job *j, const LaunchArgs &a, cudaStream_t st) {
     p.pair_blk = j->tile_box_d + j->pair_blk_off;
     p.T1f = j->t1f;
     p.Uf = j->uf;
+    p.op = 4 * j->nob;
     p.evl = j->evl_d;
     p.tiles = j->tiles;
     p.noab = (int32_t)t.noab;
@@ -1228,13 +1401,17 @@ int mixed_launch(sdt_job *j, const LaunchArgs &a, cudaStream_t st) {
     int rc = cuda_check(cudaMemsetAsync(a.queue, 0, sizeof(unsigned long long), st), "mixed form");
     if (rc) return rc;
     if (a.cluster == 4) {
-        if (type == TM_F32) rc = launch(split_fused_kernel<TM_F32, 4>);
-        else if (type == TM_BF16) rc = launch(split_fused_kernel<TM_BF16, 4>);
-        else rc = launch(split_fused_kernel<TM_F16, 4>);
+        if (type == TM_F32) rc = launch(split_fused_kernel<TM_F32, 4, 0>);
+        else if (type == TM_BF16) rc = launch(split_fused_kernel<TM_BF16, 4, 0>);
+        else rc = launch(split_fused_kernel<TM_F16, 4, 0>);
+    } else if (a.cluster == 2) {
+        if (type == TM_F32) rc = launch(split_fused_kernel<TM_F32, 1, 1>);
+        else if (type == TM_BF16) rc = launch(split_fused_kernel<TM_BF16, 1, 1>);
+        else rc = launch(split_fused_kernel<TM_F16, 1, 1>);
     } else {
-        if (type == TM_F32) rc = launch(split_fused_kernel<TM_F32, 1>);
-        else if (type == TM_BF16) rc = launch(split_fused_kernel<TM_BF16, 1>);
-        else rc = launch(split_fused_kernel<TM_F16, 1>);
+        if (type == TM_F32) rc = launch(split_fused_kernel<TM_F32, 1, 0>);
+        else if (type == TM_BF16) rc = launch(split_fused_kernel<TM_BF16, 1, 0>);
+        else rc = launch(split_fused_kernel<TM_F16, 1, 0>);
     }
     return rc;
 }

@@ -42,7 +42,7 @@ def test_choices_are_the_cheapest_and_cached(tmp_path):
     assert all(v == (4 if c == top else 1) for c, v in d["shapes"].items())
     assert cache.exists() and calls
     ctas = tuner.ctas(kl, d)
-    assert ctas.shape == (len(kl),) and set(ctas.tolist()) <= {1, 4}
+    assert ctas.shape == (len(kl),) and set(ctas.tolist()) <= {1, 2, 4}
     # a second tuner reuses the cache without timing anything
     calls.clear()
     again = autotune.Autotuner(SimpleNamespace(tiling=t), cache=cache, measure=fake).tune(kl)
