@@ -204,3 +204,20 @@ def test_fused_checkpointed_run(gpu, tmp_path):
         e = restart.CheckpointedRun(ck, kl, 9, runner).run()
         full = job.run(kl)
     assert e[0] == pytest.approx(full[0], rel=1e-13) and e[1] == pytest.approx(full[1], rel=1e-13)
+
+
+def test_restricted_tiling_both_forms(gpu):
+    """Restricted tilings (beta blocks read through their alpha twins, factor 2,
+    tce_restricted.F and ccsd_t_dot.F:52-57): FP64 and mixed forms against the oracle."""
+    t = ng.Tiling([3, 3], [4, 4], occ_spin=[1, 2], vir_spin=[1, 2], restricted=True,
+                  alpha=[1, 1, 3, 3]).with_evl(6)
+    files = ng.synth_inputs(t, 6)
+    e1, e2, pt, _ = orc.Problem(t, *files).ccsd_t()
+    kl = ng.task_list(t)
+    with ng.TriplesJob(t) as job:
+        job.load(*files)
+        g1, g2, gpt = job.run(kl, per_task=True)
+        m1, m2 = job.run(kl, precision=ng.PREC_MIXED_FP16)
+    assert g1 == pytest.approx(e1, rel=REL, abs=0) and g2 == pytest.approx(e2, rel=REL, abs=0)
+    assert np.abs(gpt - pt).max() <= REL * max(abs(e1), abs(e2))
+    assert m1 == pytest.approx(e1, rel=2e-6) and m2 == pytest.approx(e2, rel=2e-6)
