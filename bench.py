@@ -12,7 +12,8 @@ slices; one step evaluates one slice (about 22 tuples, ~7e12 FLOPs) -- all
 value: algorithmic TFLOP/s with the inputs resident in HBM (CUDA events on
 the launching stream, max over ranks).  e2e: the same metric through the
 public API with the TCE files copied from pinned host memory and the
-energies read back every step.  --impl reference times the CPU restatement
+energies read back every step (two jobs double-buffer the inputs, so step
+s+1's copies and ingest overlap step s's kernels).  --impl reference times the CPU restatement
 of the reference's (T) kernels and drivers (the oracle) on the host cores.
 Multi-GPU: each rank takes its own slices (weak scaling, no collective on
 the data path); energies are summed on the host.
@@ -225,18 +226,37 @@ def ours(args) -> None:
     value = total_flops / elapsed / 1e12
 
     # End to end through the public API: pinned-host TCE files -> device,
-    # ingest, run, energies back, every step.
-    e2e_steps = min(args.steps, 2)
+    # ingest, run, energies back, every step.  Two jobs on two streams
+    # double-buffer the inputs: while one job runs step s, a host thread
+    # loads step s+1's files into the other (the copies overlap the
+    # contraction kernel; the first step's load is not hidden).
+    e2e_steps = min(args.steps, 3)
+    job2 = ng.TriplesJob(t)
+    jobs, streams = (job, job2), (stream, torch.cuda.Stream(device=dev))
+    load_s = []
+
+    def load(k):
+        tl = time.perf_counter()
+        jobs[k].load(*files, stream=streams[k])      # returns once the ingest is done
+        load_s.append(time.perf_counter() - tl)
+
     barrier()
     t0 = time.perf_counter()
     e2e_flops = 0.0
+    load(0)
     for s in range(e2e_steps):
         ids = step_ids[args.warmup + s]
-        job.load(*files, stream=stream)
-        job.run(kl[ids], stream=stream)
+        nxt = None
+        if s + 1 < e2e_steps:
+            nxt = threading.Thread(target=load, args=((s + 1) % 2,))
+            nxt.start()
+        jobs[s % 2].run(kl[ids], stream=streams[s % 2])
+        if nxt is not None:
+            nxt.join()
         e2e_flops += step_flops[args.warmup + s]
     barrier()
     e2e_t = time.perf_counter() - t0
+    job2.close()
     if ws > 1:
         tt = torch.tensor([e2e_t, e2e_flops], dtype=torch.float64, device=dev)
         mx = tt.clone()
@@ -285,7 +305,7 @@ def ours(args) -> None:
         cpu = None
         if ws == 1 and not args.no_cpu:
             cores = os.cpu_count() or 1
-            ids, f = cpu_sample(t, files, kl, step_ids[args.warmup], float(os.environ.get("SDT_CPU_FLOPS", "3e11")))
+            ids, f = cpu_sample(t, files, kl, step_ids[args.warmup], float(os.environ.get("SDT_CPU_FLOPS", "8e11")))
             dt = run_cpu(t, files, kl, ids)
             cpu = {"value": f / dt / 1e12, "unit": "TFLOP/s", "cores": cores, "kind": "port",
                    "sample": f"{len(ids)} smallest tuples of one step slice ({f:.3e} FLOPs, {dt:.1f} s); "
@@ -310,7 +330,9 @@ def ours(args) -> None:
                          "kernel": "fused_fp64_kernel"},
             "cpu_baseline": cpu,
             "e2e": {"value": e2e, "unit": "TFLOP/s", "h2d_bytes_per_step": int(in_bytes),
-                    "d2h_bytes_per_step": 16, "steps": e2e_steps},
+                    "d2h_bytes_per_step": 16, "steps": e2e_steps, "load_s": [round(x, 4) for x in load_s],
+                    "overlap": "step s+1's files copied and ingested into a second job on its own stream "
+                               "while step s runs"},
             "gpu_launches": int(launches),
             "clocks": clocks,
             "mixed": {
@@ -478,19 +500,21 @@ def workload_sym8(args) -> None:
 
 
 def workload_serve(args) -> None:
-    """Serving stream: Poisson arrivals at 50 jobs/s, o ~ U{omin..omax},
+    """Serving stream: Poisson arrivals at `rate` jobs/s, o ~ U{omin..omax},
     v = round(o * U[5,8]), tiles from {8..32} / {16..64} (no irreps),
     inputs seeded with the job id; FIFO admission against a 150 GB HBM
     budget on `slots` workers; the mixed form (FP16x3) on every job and the
     FP64 form as a check on 1% of them.  Inputs are generated before the
     stream starts; a job's latency runs from its arrival (submission) to
-    its energies."""
+    its energies; the phase times split it into queueing (submission to
+    admission), loading (tables, copies, ingest), computing (encoding, plan,
+    kernels, sums) and the FP64 check with the job's teardown."""
     import torch
 
     import nwchem_gb300 as ng
     from nwchem_gb300 import serve
     torch.cuda.set_device(0)
-    specs = serve.job_stream(args.jobs, 50.0, 4, args.omin, args.omax)
+    specs = serve.job_stream(args.jobs, args.rate, 4, args.omin, args.omax)
     t0 = time.perf_counter()
     files = serve.prepare(specs)
     gen_s = time.perf_counter() - t0
@@ -513,6 +537,9 @@ def workload_serve(args) -> None:
         peak = srv.peak_bytes
     ok = [x for x in st if x["state"] == 2]
     lat = np.array([x["finished"] - x["submitted"] for x in ok])
+    phase = {k: np.array([x[b] - x[a] for x in ok]) for k, a, b in (
+        ("queue", "submitted", "admitted"), ("load", "admitted", "loaded"), ("compute", "loaded", "ran"),
+        ("check_and_free", "ran", "finished"), ("service", "admitted", "finished"))}
     span = max(x["finished"] for x in ok) - min(x["submitted"] for x in ok)
     flops = sum(ng.flops(s.tiling, ng.task_list(s.tiling)) for s, x in zip(specs, st) if x["state"] == 2)
     chk = [x for x, c in zip(st, check) if c and x["state"] == 2]
@@ -520,12 +547,15 @@ def workload_serve(args) -> None:
     aerr = [abs(x["energy"][1] - x["fp64"][1]) for x in chk]
     empty = sum(1 for s in specs if len(ng.task_list(s.tiling)) == 0)
     print(json.dumps({
-        "workload": f"serving: {args.jobs} jobs, Poisson 50 jobs/s, o ~ U{{{args.omin}..{args.omax}}}, "
+        "workload": f"serving: {args.jobs} jobs, Poisson {args.rate:g} jobs/s, o ~ U{{{args.omin}..{args.omax}}}, "
                     f"v = round(o*U[5,8]), tiles {{8..32}}/{{16..64}}, seed = job id",
         "slots": args.slots, "max_ctas": args.max_ctas, "budget_bytes": budget, "peak_admitted_bytes": peak,
         "jobs_done": len(ok), "jobs_failed": len(st) - len(ok),
         "jobs_per_s": len(ok) / span, "span_s": span, "p50_latency_s": float(np.percentile(lat, 50)),
         "p99_latency_s": float(np.percentile(lat, 99)), "mean_latency_s": float(lat.mean()),
+        "offered_jobs_per_s": len(specs) / specs[-1].arrival,
+        "phase_p50_s": {k: float(np.percentile(v, 50)) for k, v in phase.items()},
+        "phase_p99_s": {k: float(np.percentile(v, 99)) for k, v in phase.items()},
         "tflops": flops / span / 1e12, "fp64_checked": len(chk), "jobs_without_tuples": empty,
         "max_rel_err_E(T)_vs_fp64": max(errs) if errs else None, "max_abs_err_E(T)_vs_fp64_Eh": max(aerr) if aerr else None,
         "input_generation_s": gen_s}), flush=True)
@@ -542,8 +572,9 @@ def main() -> None:
     ap.add_argument("--tuples", type=int, default=2, help="tuples in the --profile case")
     ap.add_argument("--workload", default="o40v300", choices=["o40v300", "o64v512", "sym8", "serve"])
     ap.add_argument("--jobs", type=int, default=200, help="serve: jobs in the stream")
+    ap.add_argument("--rate", type=float, default=50.0, help="serve: Poisson arrival rate (jobs/s)")
     ap.add_argument("--omin", type=int, default=8, help="serve: smallest occupied size")
-    ap.add_argument("--omax", type=int, default=24, help="serve: largest occupied size")
+    ap.add_argument("--omax", type=int, default=16, help="serve: largest occupied size")
     ap.add_argument("--slots", type=int, default=4, help="serve: worker slots")
     ap.add_argument("--max-ctas", type=int, default=0, help="serve: CTA cap per job launch (0: all SMs)")
     ap.add_argument("--case", default="o40v114", choices=["o40v114", "o64v128", "sym8s"], help="--profile case")

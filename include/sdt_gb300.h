@@ -284,7 +284,8 @@ int sdt_server_submit(sdt_server *server, const sdt_tiling *t,
                       int64_t *ticket);
 /* state 0 queued, 1 running, 2 done, -1 failed (the job's error code is
  * returned and its message copied to msg); energy[2], fp64[2] (check) and
- * times[3] (submitted, admitted, finished) may be NULL. */
+ * times[5] (submitted, admitted, inputs on the device, energies ready,
+ * finished) may be NULL. */
 int sdt_server_status(sdt_server *server, int64_t ticket, int *state,
                       double *energy, double *fp64, double *times,
                       char *msg, size_t len);

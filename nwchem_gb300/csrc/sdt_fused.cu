@@ -31,6 +31,8 @@
 #include <cstring>
 #include <vector>
 
+#include <unistd.h>
+
 namespace sdt {
 namespace {
 
@@ -507,6 +509,27 @@ extern "C" int64_t sdt_job_device_bytes(const sdt_job *j) {
     return b;
 }
 
+// One read per host page of a buffer, just before the copy engines read it.
+// Measured on GB300 (Grace host): copies of pinned pages the CPU had not
+// touched for 8-40 s ran at 6-70 GB/s, and at ~200 GB/s right after one CPU
+// read per page (the copy path depends on per-page state the CPU refreshes);
+// the pass costs about a millisecond per 5 GB.
+static void touch_host_pages(const void *p, size_t bytes) {
+    static const size_t pg = [] {
+        const long v = sysconf(_SC_PAGESIZE);
+        return v > 0 ? (size_t)v : (size_t)4096;
+    }();
+    if (!bytes) return;
+    const volatile unsigned char *c = (const volatile unsigned char *)p;
+    // the buffer's first byte, then the first byte of every later page it spans
+    const size_t first = (size_t)((((uintptr_t)p + pg) & ~(uintptr_t)(pg - 1)) - (uintptr_t)p);
+    const int64_t n = bytes > first ? (int64_t)((bytes - first + pg - 1) / pg) : 0;
+    unsigned sum = c[0];
+#pragma omp parallel for reduction(+ : sum) num_threads(8) schedule(static) if (n > 4096)
+    for (int64_t i = 0; i < n; ++i) sum += c[first + (size_t)i * pg];
+    (void)sum;
+}
+
 extern "C" int sdt_job_load(sdt_job *j, const sdt_file *f1, const sdt_file *f2,
                             const sdt_file *fv, void *stream) {
     if (!j || !f1 || !f2 || !fv || !f1->hash || !f2->hash || !fv->hash)
@@ -514,6 +537,7 @@ extern "C" int sdt_job_load(sdt_job *j, const sdt_file *f1, const sdt_file *f2,
     cudaStream_t st = stream ? (cudaStream_t)stream : j->stream;
     const Tiling &t = j->t;
     const int64_t o = t.nocc, v = t.nvir, noab = t.noab, nvab = t.nvab, N = noab + nvab;
+    PhaseTrace tr("sdt_job_load");
 
     // Virtual tile-pair regions of Vd2.
     std::vector<int64_t> pair(nvab * nvab, -1);
@@ -529,19 +553,6 @@ extern "C" int sdt_job_load(sdt_job *j, const sdt_file *f1, const sdt_file *f2,
     mixed_release(j);
     j->loaded = false;
     j->pair_host = pair;
-    for (int a = 0; a < DST_N; ++a) {
-        j->arr[a] = (double *)gpu_get(want[a] * sizeof(double));
-        if (!j->arr[a]) {
-            job_free_arrays(j);
-            return fail(SDT_ERR_NOMEM, "sdt_job_load: dense operand allocation");
-        }
-        j->arr_n[a] = want[a];
-        int rc = cuda_check(cudaMemsetAsync(j->arr[a], 0, want[a] * sizeof(double), st), "sdt_job_load");
-        if (rc) return rc;
-    }
-    int rc = cuda_check(cudaMemcpyAsync(j->pair_off, pair.data(), pair.size() * sizeof(int64_t),
-                                        cudaMemcpyHostToDevice, st), "sdt_job_load");
-    if (rc) return rc;
 
     // Copy jobs, destination-driven: every canonical block the path can
     // read is looked up by its (restricted-mapped) key.
@@ -657,22 +668,43 @@ extern "C" int sdt_job_load(sdt_job *j, const sdt_file *f1, const sdt_file *f2,
         return fail(SDT_ERR_MISSING, "sdt_job_load: a block the path reads is absent (" + missing + ")");
     }
 
-    // Raw files to the device, then one ingest launch per 65535 jobs.
+    tr.mark("copy lists", nullptr);
+    // Raw files to the device first (copy engines only: they overlap kernels
+    // of other streams), then the clears of the dense arrays and the ingest
+    // (one launch per 65535 copy jobs), which need SMs.
     const sdt_file *files[3] = {f1, f2, fv};
     double *raw[3] = {nullptr, nullptr, nullptr};
+    int rc = SDT_OK;
     for (int f = 0; f < 3; ++f) {
         raw[f] = (double *)gpu_get((size_t)std::max<int64_t>(files[f]->ndata, 1) * sizeof(double));
         if (!raw[f]) {
             for (int g = 0; g < f; ++g) gpu_put(raw[g]);
-            job_free_arrays(j);
             return fail(SDT_ERR_NOMEM, "sdt_job_load: raw file allocation");
         }
         if (files[f]->ndata > 0) {
+            touch_host_pages(files[f]->data, (size_t)files[f]->ndata * sizeof(double));
             rc = cuda_check(cudaMemcpyAsync(raw[f], files[f]->data, (size_t)files[f]->ndata * sizeof(double),
                                             cudaMemcpyHostToDevice, st), "sdt_job_load");
             if (rc) return rc;
         }
+        tr.mark(f == 0 ? "file T1" : f == 1 ? "file T2" : "file V2", st);
     }
+    for (int a = 0; a < DST_N; ++a) {
+        j->arr[a] = (double *)gpu_get(want[a] * sizeof(double));
+        if (!j->arr[a]) {
+            cudaStreamSynchronize(st);
+            for (int f = 0; f < 3; ++f) gpu_put(raw[f]);
+            job_free_arrays(j);
+            return fail(SDT_ERR_NOMEM, "sdt_job_load: dense operand allocation");
+        }
+        j->arr_n[a] = want[a];
+        rc = cuda_check(cudaMemsetAsync(j->arr[a], 0, want[a] * sizeof(double), st), "sdt_job_load");
+        if (rc) return rc;
+    }
+    rc = cuda_check(cudaMemcpyAsync(j->pair_off, pair.data(), pair.size() * sizeof(int64_t),
+                                    cudaMemcpyHostToDevice, st), "sdt_job_load");
+    if (rc) return rc;
+    tr.mark("allocate+clear", st);
     CopyJob *jobs_d = (CopyJob *)gpu_get(std::max<size_t>(jobs.size(), 1) * sizeof(CopyJob));
     if (!jobs_d) return fail(SDT_ERR_NOMEM, "sdt_job_load: job list");
     rc = cuda_check(cudaMemcpyAsync(jobs_d, jobs.data(), jobs.size() * sizeof(CopyJob),
@@ -690,6 +722,7 @@ extern "C" int sdt_job_load(sdt_job *j, const sdt_file *f1, const sdt_file *f2,
     rc = cuda_check(cudaGetLastError(), "sdt_job_load: ingest");
     // The raw copies and the job list are released once the stream is done.
     cudaError_t e = cudaStreamSynchronize(st);
+    tr.mark("ingest", nullptr);
     for (int f = 0; f < 3; ++f) gpu_put(raw[f]);
     gpu_put(jobs_d);
     if (rc) return rc;

@@ -18,6 +18,19 @@ int error_mode();
 extern std::atomic<int64_t> g_launches;
 inline void count_launch(int64_t n = 1) { g_launches.fetch_add(n, std::memory_order_relaxed); }
 
+// Phase tracing: with SDT_TRACE set (not "0") the job surface prints the
+// wall time of its phases to stderr, synchronising its stream between
+// phases so that device work is attributed to the phase that issued it.
+bool trace_on();
+struct PhaseTrace {
+    const char *who;
+    double t0 = 0, last = 0;
+    std::string line;
+    explicit PhaseTrace(const char *w);
+    void mark(const char *phase, void *stream);  // stream: cudaStream_t to synchronise, or null
+    ~PhaseTrace();
+};
+
 // Tiling helpers (tiles are 1-based as in tce.fh).
 struct Tiling {
     int64_t noab = 0, nvab = 0, nocc = 0, nvir = 0;

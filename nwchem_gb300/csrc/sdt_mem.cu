@@ -6,8 +6,10 @@
 // (check_device_, device_init_).
 #include "sdt_common.cuh"
 
+#include <chrono>
 #include <cstdio>
 #include <cstdlib>
+#include <cstring>
 #include <map>
 #include <mutex>
 
@@ -60,12 +62,15 @@ static void *take(std::multimap<size_t, void *> &fl, std::map<void *, size_t> &l
         return p;
     }
     void *p = nullptr;
+    PhaseTrace tr(dev ? "pool: cudaMalloc" : "pool: cudaMallocHost");
     cudaError_t e = dev ? cudaMalloc(&p, bytes) : cudaMallocHost(&p, bytes);
+    tr.mark(std::to_string(bytes).c_str(), nullptr);
     if (e != cudaSuccess) {
         cudaGetLastError();
         // Drop the cache and retry once.
         for (auto &kv : fl) dev ? cudaFree(kv.second) : cudaFreeHost(kv.second);
         fl.clear();
+        tr.mark("cache dropped", nullptr);
         e = dev ? cudaMalloc(&p, bytes) : cudaMallocHost(&p, bytes);
         if (e != cudaSuccess) {
             cudaGetLastError();
@@ -143,6 +148,36 @@ int reduce_pairs(const double *partials, int64_t n, double *out_dev, cudaStream_
     reduce_pairs_kernel<<<1, 256, 0, st>>>(partials, n, out_dev);
     count_launch();
     return cuda_check(cudaGetLastError(), "reduce_pairs");
+}
+
+bool trace_on() {
+    static const bool on = [] {
+        const char *v = std::getenv("SDT_TRACE");
+        return v && *v && std::strcmp(v, "0") != 0;
+    }();
+    return on;
+}
+
+static double wall_s() {
+    return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+PhaseTrace::PhaseTrace(const char *w) : who(w) {
+    if (trace_on()) t0 = last = wall_s();
+}
+
+void PhaseTrace::mark(const char *phase, void *stream) {
+    if (!trace_on()) return;
+    if (stream) cudaStreamSynchronize((cudaStream_t)stream);
+    const double t = wall_s();
+    char buf[96];
+    std::snprintf(buf, sizeof(buf), " %s %.3f ms", phase, 1e3 * (t - last));
+    line += buf;
+    last = t;
+}
+
+PhaseTrace::~PhaseTrace() {
+    if (trace_on()) std::fprintf(stderr, "[sdt trace] %s:%s; total %.3f ms\n", who, line.c_str(), 1e3 * (wall_s() - t0));
 }
 
 static int local_index() {

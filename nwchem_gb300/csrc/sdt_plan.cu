@@ -323,13 +323,16 @@ extern "C" int sdt_job_run(sdt_job *j, const int64_t *klist, int64_t n, int prec
                            double *per_task, void *stream) {
     if (!j || !energy || (n > 0 && !klist)) return fail(SDT_ERR_ARG, "sdt_job_run: null argument");
     energy[0] = energy[1] = 0.0;
+    PhaseTrace tr("sdt_job_run");
+    cudaStream_t st = stream ? (cudaStream_t)stream : j->stream;
     sdt_plan *p = nullptr;
     int rc = plan_create(j, klist, n, precision, nullptr, &p, "sdt_job_run");
     if (rc) return rc;
-    cudaStream_t st = stream ? (cudaStream_t)stream : j->stream;
+    tr.mark("plan", st);
     rc = plan_enqueue(p, st);
     if (!rc) rc = plan_read(p, st, energy, per_task, "sdt_job_run");
     else cudaStreamSynchronize(st);
+    tr.mark("kernels+sums", nullptr);
     plan_free(p);
     return rc;
 }

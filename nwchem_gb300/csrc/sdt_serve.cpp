@@ -7,7 +7,8 @@
 // jobs already admitted (a job larger than the whole budget is rejected).
 // Each slot is a worker thread; an admitted job runs on its own CUDA stream:
 // device tables, H2D copy and ingest of its files, the mixed form's operand
-// encoding, the persistent kernel over all its tuples and the energy sums,
+// encoding, the persistent kernel over all its tuples (work-unit shape chosen
+// from the job's contraction length) and the energy sums,
 // then (optionally) the FP64 form as a check, and its memory is returned.
 // Jobs admitted together overlap on the device -- one job's copies and
 // encoding with another's contraction kernel, and their kernels at launch
@@ -111,7 +112,7 @@ struct sdt_server {
         int64_t bytes = 0;
         int state = 0;  // 0 queued, 1 running, 2 done, -1 failed
         double e[2] = {0, 0}, f[2] = {0, 0};
-        double t_submit = 0, t_start = 0, t_end = 0;
+        double t_submit = 0, t_start = 0, t_loaded = 0, t_ran = 0, t_end = 0;
         int err = 0;
         std::string msg;
     };
@@ -133,6 +134,22 @@ struct sdt_server {
 
 namespace {
 
+// Work-unit shape for a job: the tensor-memory hold (2) when the contraction
+// length a sub-box sees is short -- (o + v) over the number of distinct
+// irreps below 320, where the FP64 energy work per element outweighs the
+// tensor-core work -- else the register hold (1).
+int mixed_shape(const sdt_tiling *t) {
+    int64_t o = 0, v = 0;
+    bool seen[8] = {false};
+    int nsym = 0;
+    for (int64_t b = 0; b < t->noab + t->nvab; ++b) {
+        (b < t->noab ? o : v) += t->range[b];
+        const int y = (int)(t->sym[b] & 7);
+        if (!seen[y]) seen[y] = true, ++nsym;
+    }
+    return (o + v) / std::max(nsym, 1) < 320 ? 2 : 1;
+}
+
 void run_one(sdt_server *s, sdt_server::Job *job) {
     cudaSetDevice(s->device);
     sdt_job *j = nullptr;
@@ -149,7 +166,9 @@ void run_one(sdt_server *s, sdt_server::Job *job) {
         return;
     }
     if (s->max_ctas > 0) sdt_job_set_max_ctas(j, s->max_ctas);
+    if (job->precision != SDT_PREC_FP64) sdt_job_set_mixed_cluster(j, mixed_shape(&job->t));
     rc = sdt_job_load(j, &job->f1, &job->f2, &job->fv, nullptr);
+    job->t_loaded = s->now();
     std::vector<int64_t> kl;
     int64_t n = 0;
     if (!rc) {
@@ -158,6 +177,7 @@ void run_one(sdt_server *s, sdt_server::Job *job) {
         rc = n < 0 ? SDT_ERR_ARG : sdt_tasks_list(&job->t, n, kl.data());
     }
     if (!rc) rc = sdt_job_run(j, kl.data(), n, job->precision, job->e, nullptr, nullptr);
+    job->t_ran = s->now();
     if (!rc && job->check) rc = sdt_job_run(j, kl.data(), n, SDT_PREC_FP64, job->f, nullptr, nullptr);
     if (rc) failed(rc);
     sdt_job_destroy(j);
@@ -257,8 +277,11 @@ extern "C" int sdt_server_submit(sdt_server *s, const sdt_tiling *t, const sdt_f
 
 // state: 0 queued, 1 running, 2 done, -1 failed (sdt_last_error-style message
 // in msg when given).  energy: the job's (E[T], E(T)); fp64: the FP64 check
-// (when requested); times: submit, admission and completion in seconds since
-// the server was created.
+// (when requested); times (5 values, seconds since the server was created):
+// submission, admission, inputs on the device (job tables built, files
+// copied and ingested), energies of the requested precision ready (operand
+// encoding, plan and kernels done), and completion (after the FP64 check
+// when one was requested, and the job's memory returned).
 extern "C" int sdt_server_status(sdt_server *s, int64_t ticket, int *state, double *energy, double *fp64,
                                  double *times, char *msg, size_t len) {
     if (!s || !state) return fail(SDT_ERR_ARG, "sdt_server_status: null argument");
@@ -268,7 +291,10 @@ extern "C" int sdt_server_status(sdt_server *s, int64_t ticket, int *state, doub
     *state = j.state;
     if (energy) energy[0] = j.e[0], energy[1] = j.e[1];
     if (fp64) fp64[0] = j.f[0], fp64[1] = j.f[1];
-    if (times) times[0] = j.t_submit, times[1] = j.t_start, times[2] = j.t_end;
+    if (times) {
+        times[0] = j.t_submit, times[1] = j.t_start, times[2] = j.t_loaded;
+        times[3] = j.t_ran, times[4] = j.t_end;
+    }
     if (msg && len) std::snprintf(msg, len, "%s", j.msg.c_str());
     return j.state < 0 ? j.err : SDT_OK;
 }

@@ -103,14 +103,15 @@ class Server:
 
     def status(self, ticket: int) -> dict:
         st = C.c_int()
-        e, f, tm = np.zeros(2), np.zeros(2), np.zeros(3)
+        e, f, tm = np.zeros(2), np.zeros(2), np.zeros(5)
         buf = C.create_string_buffer(512)
         rc = self._lib.sdt_server_status(self._h, int(ticket), C.byref(st), e.ctypes.data_as(_capi.PD),
                                          f.ctypes.data_as(_capi.PD), tm.ctypes.data_as(_capi.PD), buf, 512)
         if st.value in (2, -1):
             self._held.pop(ticket, None)
         return {"state": st.value, "rc": rc, "energy": (float(e[0]), float(e[1])), "fp64": (float(f[0]), float(f[1])),
-                "submitted": float(tm[0]), "admitted": float(tm[1]), "finished": float(tm[2]),
+                "submitted": float(tm[0]), "admitted": float(tm[1]), "loaded": float(tm[2]),
+                "ran": float(tm[3]), "finished": float(tm[4]),
                 "msg": buf.value.decode(errors="replace")}
 
     def drain(self, timeout: float = 3600.0) -> None:
