@@ -133,13 +133,41 @@ __device__ __forceinline__ void run_term(const FusedParams &p, const TupleCtx &t
     const int r = lane >> 2, q = lane & 3;
     const int wm = warp >> 1, wn = warp & 1;
 
+    // Order of the three row (column) indices inside the 64 GEMM rows: the
+    // one with the fewest valid values in this sub-box is outermost, so the
+    // rows past its extent are whole 16-row groups -- whole fragments, which
+    // are skipped (a ragged tile's last sub-box costs what it holds).
+    // lev_r[p]: level (0 outermost) of row index p of the term.
+    const int nr0 = min(BOX, t.ext[td.r[0]] - t.boff[td.r[0]]), nr1 = min(BOX, t.ext[td.r[1]] - t.boff[td.r[1]]),
+              nr2 = min(BOX, t.ext[td.r[2]] - t.boff[td.r[2]]);
+    const int nc0 = min(BOX, t.ext[td.c[0]] - t.boff[td.c[0]]), nc1 = min(BOX, t.ext[td.c[1]] - t.boff[td.c[1]]),
+              nc2 = min(BOX, t.ext[td.c[2]] - t.boff[td.c[2]]);
+    const int orow = nr1 < nr0 ? (nr2 < nr1 ? 2 : 1) : (nr2 < nr0 ? 2 : 0);
+    const int ocol = nc1 < nc0 ? (nc2 < nc1 ? 2 : 1) : (nc2 < nc0 ? 2 : 0);
+    const int rlive = orow == 0 ? nr0 : orow == 1 ? nr1 : nr2;
+    const int clive = ocol == 0 ? nc0 : ocol == 1 ? nc1 : nc2;
+    int lev_r[3], lev_c[3];
+#pragma unroll
+    for (int e = 0; e < 3; ++e) {
+        lev_r[e] = e == orow ? 0 : (e < orow ? e + 1 : e);
+        lev_c[e] = e == ocol ? 0 : (e < ocol ? e + 1 : e);
+    }
+    auto lat = [](int lev, int m) { return lev == 0 ? (m >> 4) : lev == 1 ? ((m >> 2) & 3) : (m & 3); };
+    // live fragments: row fragment i of this warp holds level-0 value 2*wm + i/2
+    unsigned rfrag = 0, cfrag = 0;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        rfrag |= (2 * wm + (i >> 1) < rlive) ? (1u << i) : 0u;
+        cfrag |= (2 * wn + (i >> 1) < clive) ? (1u << i) : 0u;
+    }
+
     int64_t abase[4], bbase[4];
     unsigned aok = 0, bok = 0;
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
         const int m = wm * 32 + i * 8 + r;
-        const int l0 = m >> 4, l1 = (m >> 2) & 3, l2 = m & 3;
-        const int x0 = t.boff[td.r[0]] + l0, x1 = t.boff[td.r[1]] + l1, x2 = t.boff[td.r[2]] + l2;
+        const int x0 = t.boff[td.r[0]] + lat(lev_r[0], m), x1 = t.boff[td.r[1]] + lat(lev_r[1], m),
+                  x2 = t.boff[td.r[2]] + lat(lev_r[2], m);
         const bool ok = x0 < t.ext[td.r[0]] && x1 < t.ext[td.r[1]] && x2 < t.ext[td.r[2]];
         aok |= ok ? (1u << i) : 0u;
         const int64_t g0 = t.start[td.r[0]] + x0, g1 = t.start[td.r[1]] + x1,
@@ -151,8 +179,8 @@ __device__ __forceinline__ void run_term(const FusedParams &p, const TupleCtx &t
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
         const int n = wn * 32 + j * 8 + r;
-        const int l0 = n >> 4, l1 = (n >> 2) & 3, l2 = n & 3;
-        const int x0 = t.boff[td.c[0]] + l0, x1 = t.boff[td.c[1]] + l1, x2 = t.boff[td.c[2]] + l2;
+        const int x0 = t.boff[td.c[0]] + lat(lev_c[0], n), x1 = t.boff[td.c[1]] + lat(lev_c[1], n),
+                  x2 = t.boff[td.c[2]] + lat(lev_c[2], n);
         const bool ok = x0 < t.ext[td.c[0]] && x1 < t.ext[td.c[1]] && x2 < t.ext[td.c[2]];
         bok |= ok ? (1u << j) : 0u;
         const int64_t g0 = t.start[td.c[0]] + x0, g2 = t.start[td.c[2]] + x2;
@@ -214,7 +242,9 @@ __device__ __forceinline__ void run_term(const FusedParams &p, const TupleCtx &t
 #pragma unroll
             for (int i = 0; i < 4; ++i)
 #pragma unroll
-                for (int j = 0; j < 4; ++j) dmma_8x8x4(acc[i][j][0], acc[i][j][1], a[i], b[j]);
+                for (int j = 0; j < 4; ++j)
+                    if ((rfrag >> i & 1u) && (cfrag >> j & 1u))  // warp-uniform
+                        dmma_8x8x4(acc[i][j][0], acc[i][j][1], a[i], b[j]);
         }
     }
 
@@ -224,14 +254,14 @@ __device__ __forceinline__ void run_term(const FusedParams &p, const TupleCtx &t
     for (int i = 0; i < 4; ++i) {
         if (!(aok >> i & 1u)) continue;
         const int m = wm * 32 + i * 8 + r;
-        const int roff = (m >> 4) * stride6(td.r[0]) + ((m >> 2) & 3) * stride6(td.r[1]) +
-                         (m & 3) * stride6(td.r[2]);
+        const int roff = lat(lev_r[0], m) * stride6(td.r[0]) + lat(lev_r[1], m) * stride6(td.r[1]) +
+                         lat(lev_r[2], m) * stride6(td.r[2]);
 #pragma unroll
         for (int j = 0; j < 4; ++j)
 #pragma unroll
             for (int h = 0; h < 2; ++h) {
                 const int n = wn * 32 + j * 8 + 2 * q + h;
-                const int l0 = n >> 4, l1 = (n >> 2) & 3, l2 = n & 3;
+                const int l0 = lat(lev_c[0], n), l1 = lat(lev_c[1], n), l2 = lat(lev_c[2], n);
                 if (t.boff[td.c[0]] + l0 >= t.ext[td.c[0]] || t.boff[td.c[1]] + l1 >= t.ext[td.c[1]] ||
                     t.boff[td.c[2]] + l2 >= t.ext[td.c[2]])
                     continue;
