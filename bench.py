@@ -42,7 +42,7 @@ WORKLOAD = ("o40v300 tiled FP64 drop-in: o=40 as 8/12/20, v=300 as 20,24x5,30x4,
             "step = one of 128 strided slices of the 2860-tuple weight-ordered list")
 METRIC = "(T) TFLOP/s"
 # ncu, fused_fp64_kernel on 2 tuples of o40v114 (profiles/fused_fp64_kernel_o40v114_2tuples.md)
-FP64_DRAM_BYTES_PER_FLOP = (321.5e6 + 15.5e6) / 2.587e11
+FP64_DRAM_BYTES_PER_FLOP = (327.9e6 + 26.2e6) / 2.587e11
 MIXED_FORMS = (("tf32", 1), ("bf16", 2), ("fp16", 3))
 MIXED_NOTE = {"tf32": "TF32x3: TF32 hi/lo pairs, kind::tf32", "bf16": "BF16x3: bf16 hi/lo pairs, kind::f16",
               "fp16": "FP16x3: fp16 hi/lo pairs of power-of-two scaled operands, kind::f16",
@@ -323,7 +323,7 @@ def ours(args) -> None:
                          "frac": achieved / peak if peak > 0 else None,
                          "traffic": FP64_DRAM_BYTES_PER_FLOP * my_flops / args.steps,
                          "traffic_note": "dram read+write bytes per launch, scaled by FLOPs from the ncu capture "
-                                         "of the 2-tuple o40v114 case (337 MB for 2.587e11 FLOPs; operands stay "
+                                         "of the 2-tuple o40v114 case (354 MB for 2.587e11 FLOPs; operands stay "
                                          "L2-resident, so traffic grows with the work, not with reuse)",
                          "peak_source": "measured in-run: FP64 mma.sync m8n8k4 probe (no FP64 entry in "
                                         "MEASURED_PEAKS.json)",
