@@ -270,8 +270,10 @@ int64_t sdt_plan_items(const sdt_plan *plan);
  * `slots` workers is free and sdt_job_bytes of the job fits in the byte
  * budget minus the admitted jobs' bytes (a job larger than the budget
  * fails with SDT_ERR_NOMEM); each admitted job runs on its own stream --
- * create, load, the given precision over all its tuples, optionally the
- * FP64 form as a check -- so admitted jobs overlap on the device.
+ * create, load, the given precision over all its tuples -- so admitted
+ * jobs overlap on the device.  A job submitted with check_fp64 keeps its
+ * device memory after its energies are delivered (state 3) and runs the
+ * FP64 form as a check when no admissible job is waiting.
  * max_ctas (0: all SMs) caps the CTAs of each job's persistent launches.
  * The caller keeps a job's files alive until its state is 2 (done) or -1
  * (failed).  Times are seconds since sdt_server_create. */
@@ -282,13 +284,17 @@ int sdt_server_submit(sdt_server *server, const sdt_tiling *t,
                       const sdt_file *t1, const sdt_file *t2,
                       const sdt_file *v2, int precision, int check_fp64,
                       int64_t *ticket);
-/* state 0 queued, 1 running, 2 done, -1 failed (the job's error code is
+/* state 0 queued, 1 running, 3 energies ready with the FP64 check pending,
+ * 2 done, -1 failed (the job's error code is
  * returned and its message copied to msg); energy[2], fp64[2] (check) and
  * times[5] (submitted, admitted, inputs on the device, energies ready,
  * finished) may be NULL. */
 int sdt_server_status(sdt_server *server, int64_t ticket, int *state,
                       double *energy, double *fp64, double *times,
                       char *msg, size_t len);
+/* CTAs of each deferred FP64 check (default a quarter of the SMs); while a
+ * check runs, mixed jobs launch on the remaining SMs.  0: no cap. */
+int sdt_server_set_check_ctas(sdt_server *server, int ctas);
 int sdt_server_drain(sdt_server *server, double timeout_s);
 int64_t sdt_server_peak_bytes(sdt_server *server);
 int sdt_server_destroy(sdt_server *server);
@@ -302,8 +308,12 @@ int sdt_admission_simulate(int64_t n, const double *arrival,
                            const int64_t *bytes, const double *service,
                            int64_t budget, int slots, double *start,
                            double *end);
-/* Caps the CTAs of a job's persistent launches (0: all SMs). */
+/* Caps a job's persistent launches at `ctas` SMs' worth of CTAs (0: all
+ * SMs; a mixed launch runs one CTA per SM, an FP64 launch up to four). */
 int sdt_job_set_max_ctas(sdt_job *job, int ctas);
+/* FP64 persistent launches with one CTA per SM (on != 0): a launch capped
+ * by sdt_job_set_max_ctas then occupies exactly that many SMs. */
+int sdt_job_set_sm_exclusive(sdt_job *job, int on);
 /* The job's own stream (the default stream of its calls). */
 void *sdt_job_stream(const sdt_job *job);
 

@@ -73,6 +73,8 @@ def _declare(lib):
         "sdt_server_status": (C.c_int, [C.c_void_p, C.c_int64, C.POINTER(C.c_int), PD, PD, PD, C.c_char_p,
                                         C.c_size_t]),
         "sdt_server_drain": (C.c_int, [C.c_void_p, C.c_double]),
+        "sdt_server_set_check_ctas": (C.c_int, [C.c_void_p, C.c_int]),
+        "sdt_job_set_sm_exclusive": (C.c_int, [C.c_void_p, C.c_int]),
         "sdt_server_peak_bytes": (C.c_int64, [C.c_void_p]),
         "sdt_server_destroy": (C.c_int, [C.c_void_p]),
         "sdt_job_bytes": (C.c_int64, [C.POINTER(SdtTiling), C.c_int]),

@@ -415,10 +415,18 @@ int tuple_sums(const double *part, const int64_t *gpref, int64_t n, double *task
     return reduce_pairs(task, n, out, st);
 }
 
+// Dynamic shared memory (unused by the kernel) that a launch requests to
+// keep one CTA per SM: with the 36.9 KB static part, two no longer fit.
+constexpr int kExclusiveSmem = 96 * 1024;
+
 int fp64_grid(sdt_job *j, int64_t items, int *grid) {
     int nsm = 0, per_sm = 0;
     int rc = cuda_check(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, j->dev), "FP64 form");
-    if (!rc) rc = cuda_check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fused_fp64_kernel, kThreads, 0),
+    if (!rc && j->sm_exclusive)
+        rc = cuda_check(cudaFuncSetAttribute(fused_fp64_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             kExclusiveSmem), "FP64 form");
+    if (!rc) rc = cuda_check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fused_fp64_kernel, kThreads,
+                                                                           j->sm_exclusive ? kExclusiveSmem : 0),
                              "FP64 form");
     if (rc) return rc;
     int64_t cap = (int64_t)nsm * std::max(per_sm, 1);
@@ -444,7 +452,7 @@ int fp64_launch(sdt_job *j, const LaunchArgs &a, cudaStream_t st) {
     p.queue = a.queue;
     int rc = cuda_check(cudaMemsetAsync(a.queue, 0, sizeof(unsigned long long), st), "FP64 form");
     if (rc) return rc;
-    fused_fp64_kernel<<<(unsigned)a.grid, kThreads, 0, st>>>(p);
+    fused_fp64_kernel<<<(unsigned)a.grid, kThreads, j->sm_exclusive ? kExclusiveSmem : 0, st>>>(p);
     count_launch();
     return cuda_check(cudaGetLastError(), "FP64 form: fused kernel");
 }
@@ -818,6 +826,15 @@ extern "C" int sdt_job_set_timing(sdt_job *j, int on) {
 }
 
 extern "C" double sdt_job_last_kernel_ms(const sdt_job *j) { return j ? (double)j->last_ms : -1.0; }
+
+// FP64 persistent launches with one CTA per SM (on): a launch capped by
+// sdt_job_set_max_ctas then occupies exactly that many SMs and leaves the
+// others whole for kernels of other streams.
+extern "C" int sdt_job_set_sm_exclusive(sdt_job *j, int on) {
+    if (!j) return fail(SDT_ERR_ARG, "sdt_job_set_sm_exclusive: null job");
+    j->sm_exclusive = on ? 1 : 0;
+    return SDT_OK;
+}
 
 extern "C" int sdt_job_set_max_ctas(sdt_job *j, int sms) {
     if (!j || sms < 0) return fail(SDT_ERR_ARG, "sdt_job_set_max_ctas: bad argument");

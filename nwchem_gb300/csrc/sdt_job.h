@@ -21,6 +21,7 @@ struct sdt_job {
     int dev = 0;
     cudaStream_t stream = nullptr;       // the job's own stream (default for its work)
     int max_ctas = 0;                    // cap on the CTAs of its persistent launches (0: all SMs)
+    int sm_exclusive = 0;                // FP64 persistent launches: one CTA per SM
     // device
     int32_t *tiles = nullptr;
     double *evl_d = nullptr;

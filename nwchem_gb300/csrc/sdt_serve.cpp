@@ -8,8 +8,10 @@
 // Each slot is a worker thread; an admitted job runs on its own CUDA stream:
 // device tables, H2D copy and ingest of its files, the mixed form's operand
 // encoding, the persistent kernel over all its tuples (work-unit shape chosen
-// from the job's contraction length) and the energy sums,
-// then (optionally) the FP64 form as a check, and its memory is returned.
+// from the job's contraction length) and the energy sums, and its memory is
+// returned.  A job with an FP64 check keeps its device memory (and its
+// admitted bytes) after its energies are delivered; the check runs when no
+// admissible job is waiting, so checks do not hold back the stream.
 // Jobs admitted together overlap on the device -- one job's copies and
 // encoding with another's contraction kernel, and their kernels at launch
 // boundaries (or throughout, with max_ctas capping each job's CTAs).  A
@@ -47,6 +49,9 @@ struct Admission {
         --busy;
         in_use -= bytes;
     }
+    // A job held for its deferred FP64 check keeps its bytes but no slot.
+    void free_slot() { --busy; }
+    void take_slot() { ++busy; }
 };
 
 int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
@@ -110,17 +115,21 @@ struct sdt_server {
         sdt_file f1{}, f2{}, fv{};
         int precision = SDT_PREC_MIXED_FP16, check = 0;
         int64_t bytes = 0;
-        int state = 0;  // 0 queued, 1 running, 2 done, -1 failed
+        int state = 0;  // 0 queued, 1 running, 3 energies ready (FP64 check pending), 2 done, -1 failed
         double e[2] = {0, 0}, f[2] = {0, 0};
         double t_submit = 0, t_start = 0, t_loaded = 0, t_ran = 0, t_end = 0;
         int err = 0;
         std::string msg;
+        sdt_job *held = nullptr;  // kept on the device for the deferred FP64 check
+        std::vector<int64_t> kl;
     };
     int64_t budget = 0;
     int slots = 1, max_ctas = 0;
+    int sms = 0, check_ctas = 0, checks_running = 0;
     std::mutex mu;
     std::condition_variable cv;
     std::deque<Job *> queue;
+    std::deque<Job *> checks;  // energies delivered, FP64 check pending (FIFO)
     std::vector<std::unique_ptr<Job>> jobs;
     Admission adm;
     std::vector<std::thread> workers;
@@ -165,32 +174,85 @@ void run_one(sdt_server *s, sdt_server::Job *job) {
         failed(rc);
         return;
     }
-    if (s->max_ctas > 0) sdt_job_set_max_ctas(j, s->max_ctas);
     if (job->precision != SDT_PREC_FP64) sdt_job_set_mixed_cluster(j, mixed_shape(&job->t));
     rc = sdt_job_load(j, &job->f1, &job->f2, &job->fv, nullptr);
     job->t_loaded = s->now();
-    std::vector<int64_t> kl;
     int64_t n = 0;
     if (!rc) {
         n = sdt_tasks_count(&job->t);
-        kl.resize(7 * std::max<int64_t>(n, 1));
-        rc = n < 0 ? SDT_ERR_ARG : sdt_tasks_list(&job->t, n, kl.data());
+        job->kl.resize(7 * std::max<int64_t>(n, 1));
+        rc = n < 0 ? SDT_ERR_ARG : sdt_tasks_list(&job->t, n, job->kl.data());
+        if (!rc) job->kl.resize(7 * n);
     }
-    if (!rc) rc = sdt_job_run(j, kl.data(), n, job->precision, job->e, nullptr, nullptr);
+    if (!rc) {
+        // While an FP64 check holds check_ctas SMs, launch on the others (a
+        // persistent launch wider than the free SMs would end only after
+        // the check).
+        int cap = s->max_ctas;
+        {
+            std::lock_guard<std::mutex> lk(s->mu);
+            if (s->checks_running > 0 && s->check_ctas > 0) {
+                const int free_sms = std::max(s->sms - s->check_ctas * s->checks_running, 1);
+                cap = cap > 0 ? std::min(cap, free_sms) : free_sms;
+            }
+        }
+        sdt_job_set_max_ctas(j, cap);
+        rc = sdt_job_run(j, job->kl.data(), n, job->precision, job->e, nullptr, nullptr);
+    }
     job->t_ran = s->now();
-    if (!rc && job->check) rc = sdt_job_run(j, kl.data(), n, SDT_PREC_FP64, job->f, nullptr, nullptr);
+    if (!rc && job->check) {
+        job->held = j;  // the FP64 check runs later, when no admissible job waits
+        return;
+    }
     if (rc) failed(rc);
     sdt_job_destroy(j);
 }
 
+// The deferred FP64 check of a held job, then its device memory is returned.
+void run_check(sdt_server *s, sdt_server::Job *job) {
+    cudaSetDevice(s->device);
+    const int64_t n = (int64_t)job->kl.size() / 7;
+    sdt_job_set_sm_exclusive(job->held, s->check_ctas > 0);  // exactly check_ctas SMs; 0: all of them
+    sdt_job_set_max_ctas(job->held, s->check_ctas);
+    const int rc = sdt_job_run(job->held, job->kl.data(), n, SDT_PREC_FP64, job->f, nullptr, nullptr);
+    if (rc) {
+        char buf[512] = {0};
+        sdt_last_error(buf, sizeof(buf));
+        job->err = rc;
+        job->msg = buf;
+    }
+    sdt_job_destroy(job->held);
+    job->held = nullptr;
+}
+
+// Workers take the queue head when it can be admitted (or must be refused);
+// otherwise, and only then, a pending FP64 check -- so checks fill the gaps
+// instead of holding the GPU while admissible jobs wait.
 void worker(sdt_server *s) {
     std::unique_lock<std::mutex> lk(s->mu);
+    auto head_ready = [&] {
+        return !s->queue.empty() &&
+               (!s->adm.fits_ever(s->queue.front()->bytes) || s->adm.can_admit(s->queue.front()->bytes));
+    };
+    auto check_ready = [&] { return !s->checks.empty() && s->adm.busy < s->adm.slots && !head_ready(); };
     while (true) {
-        s->cv.wait(lk, [&] {
-            return s->stop || (!s->queue.empty() && (!s->adm.fits_ever(s->queue.front()->bytes) ||
-                                                     s->adm.can_admit(s->queue.front()->bytes)));
-        });
+        s->cv.wait(lk, [&] { return s->stop || head_ready() || check_ready(); });
         if (s->stop) return;
+        if (!head_ready()) {
+            sdt_server::Job *job = s->checks.front();
+            s->checks.pop_front();
+            s->adm.take_slot();
+            ++s->checks_running;
+            lk.unlock();
+            run_check(s, job);
+            lk.lock();
+            --s->checks_running;
+            s->adm.release(job->bytes);
+            job->t_end = s->now();
+            job->state = job->err ? -1 : 2;
+            s->cv.notify_all();
+            continue;
+        }
         sdt_server::Job *job = s->queue.front();
         s->queue.pop_front();
         if (!s->adm.fits_ever(job->bytes)) {
@@ -207,9 +269,15 @@ void worker(sdt_server *s) {
         lk.unlock();
         run_one(s, job);
         lk.lock();
-        s->adm.release(job->bytes);
-        job->t_end = s->now();
-        job->state = job->err ? -1 : 2;
+        if (job->held) {  // energies delivered; memory kept for the check
+            s->adm.free_slot();
+            job->state = 3;
+            s->checks.push_back(job);
+        } else {
+            s->adm.release(job->bytes);
+            job->t_end = s->now();
+            job->state = job->err ? -1 : 2;
+        }
         s->cv.notify_all();
     }
 }
@@ -231,8 +299,23 @@ extern "C" int sdt_server_create(int64_t budget_bytes, int slots, int max_ctas, 
     s->adm.budget = budget_bytes;
     s->adm.slots = slots;
     cudaGetDevice(&s->device);
+    if (cudaDeviceGetAttribute(&s->sms, cudaDevAttrMultiProcessorCount, s->device) != cudaSuccess) {
+        cudaGetLastError();
+        s->sms = 0;
+    }
+    s->check_ctas = s->sms / 4;
     for (int k = 0; k < slots; ++k) s->workers.emplace_back(worker, s);
     *out = s;
+    return SDT_OK;
+}
+
+// SMs of each deferred FP64 check's persistent launch (default: a quarter
+// of them, one CTA per SM); while checks run, mixed jobs launch on the
+// remaining SMs.  0: checks use the whole GPU and do not cap other jobs.
+extern "C" int sdt_server_set_check_ctas(sdt_server *s, int ctas) {
+    if (!s || ctas < 0) return fail(SDT_ERR_ARG, "sdt_server_set_check_ctas: bad argument");
+    std::lock_guard<std::mutex> lk(s->mu);
+    s->check_ctas = s->sms > 0 ? std::min(ctas, s->sms - 1) : ctas;
     return SDT_OK;
 }
 
@@ -275,8 +358,8 @@ extern "C" int sdt_server_submit(sdt_server *s, const sdt_tiling *t, const sdt_f
     return SDT_OK;
 }
 
-// state: 0 queued, 1 running, 2 done, -1 failed (sdt_last_error-style message
-// in msg when given).  energy: the job's (E[T], E(T)); fp64: the FP64 check
+// state: 0 queued, 1 running, 3 energies ready with the FP64 check pending,
+// 2 done, -1 failed (sdt_last_error-style message in msg when given).  energy: the job's (E[T], E(T)); fp64: the FP64 check
 // (when requested); times (5 values, seconds since the server was created):
 // submission, admission, inputs on the device (job tables built, files
 // copied and ingested), energies of the requested precision ready (operand
@@ -304,10 +387,7 @@ extern "C" int sdt_server_status(sdt_server *s, int64_t ticket, int *state, doub
 extern "C" int sdt_server_drain(sdt_server *s, double timeout_s) {
     if (!s) return fail(SDT_ERR_ARG, "sdt_server_drain: null server");
     std::unique_lock<std::mutex> lk(s->mu);
-    auto done = [&] {
-        if (!s->queue.empty() || s->adm.busy) return false;
-        return true;
-    };
+    auto done = [&] { return s->queue.empty() && s->checks.empty() && !s->adm.busy; };
     if (!s->cv.wait_for(lk, std::chrono::duration<double>(timeout_s), done))
         return fail(SDT_ERR_TIMEOUT, "sdt_server_drain: jobs still running");
     return SDT_OK;
@@ -319,7 +399,8 @@ extern "C" int64_t sdt_server_peak_bytes(sdt_server *s) {
     return s->adm.peak;
 }
 
-// Stops the workers after their running jobs; queued jobs are dropped.
+// Stops the workers after their running jobs; queued jobs and pending FP64
+// checks are dropped (the held jobs' memory is returned).
 extern "C" int sdt_server_destroy(sdt_server *s) {
     if (!s) return SDT_OK;
     {
@@ -328,6 +409,11 @@ extern "C" int sdt_server_destroy(sdt_server *s) {
         s->cv.notify_all();
     }
     for (auto &w : s->workers) w.join();
+    for (auto &job : s->jobs)
+        if (job->held) {
+            sdt_job_destroy(job->held);
+            job->held = nullptr;
+        }
     delete s;
     return SDT_OK;
 }

@@ -1124,6 +1124,7 @@ void mixed_release(sdt_job *j) {
 
 int mixed_prepare(sdt_job *j, int type, cudaStream_t st) {
     mixed_release(j);
+    PhaseTrace tr("mixed_prepare");
     const Tiling &t = j->t;
     const int64_t o = t.nocc, v = t.nvir, noab = t.noab, nvab = t.nvab, nt = noab + nvab;
     const int es = type == TM_F32 ? 4 : 2;
@@ -1156,6 +1157,7 @@ int mixed_prepare(sdt_job *j, int type, cudaStream_t st) {
         sT = fp16_scale(m[0]);
         sI = fp16_scale(std::max(m[1], m[2]));
     }
+    tr.mark("scales", st);
     j->inv_s = 1.0 / (sT * sI);
     j->inv_s2 = j->inv_s * j->inv_s;
     // Every K tile is allowed for every term when all tiles share one spin and one irrep.
@@ -1223,6 +1225,7 @@ int mixed_prepare(sdt_job *j, int type, cudaStream_t st) {
                     "mixed form: tables");
     j->tile_box_off = (int64_t)o_tbox;
     j->pair_blk_off = (int64_t)o_pairblk;
+    tr.mark("tables", st);
     // Block-major split operands.
     const int64_t nblk[L_N] = {NVB * NOB * NOB * nko, NVB * NOB * NOB * nkv, NVB * NVB * NOB * nko, nvd2};
     const int srcidx[L_N] = {DST_WD1, DST_T2B, DST_T2A, DST_VD2};
@@ -1268,6 +1271,7 @@ int mixed_prepare(sdt_job *j, int type, cudaStream_t st) {
         else pack_blocks_kernel<TM_F16><<<gb, 256, 0, st>>>(g);
         count_launch();
     }
+    tr.mark("pack", st);
     // FP32 copies of T1 [v][OP] and the vvoo block [v][v][OP][OP] for the s1
     // terms, holes padded per tile to multiples of 4.
     const int64_t OP = 4 * NOB;
@@ -1289,6 +1293,7 @@ int mixed_prepare(sdt_job *j, int type, cudaStream_t st) {
         rc = cuda_check(cudaGetLastError(), "mixed form: split");
     }
     if (!rc) rc = cuda_check(cudaStreamSynchronize(st), "mixed form: prepare");
+    tr.mark("fp32 copies", nullptr);
     if (rc) {
         mixed_release(j);
         return rc;

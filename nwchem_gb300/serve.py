@@ -82,12 +82,14 @@ class _Held:
 
 
 class Server:
-    def __init__(self, budget_bytes: int, slots: int = 4, max_ctas: int = 0):
+    def __init__(self, budget_bytes: int, slots: int = 4, max_ctas: int = 0, check_ctas: int | None = None):
         self._lib = _capi.lib()
         h = C.c_void_p()
         _capi.check(self._lib.sdt_server_create(int(budget_bytes), int(slots), int(max_ctas), C.byref(h)),
                     "sdt_server_create")
         self._h = h
+        if check_ctas is not None:   # default: a quarter of the SMs for each deferred FP64 check
+            _capi.check(self._lib.sdt_server_set_check_ctas(h, int(check_ctas)), "sdt_server_set_check_ctas")
         self._held: dict[int, _Held] = {}
 
     def submit(self, tiling: Tiling, files: tuple[TceFile, TceFile, TceFile], precision: int = PREC_MIXED_FP16,

@@ -138,6 +138,13 @@ class TriplesJob:
         (8 TF32 or 16 BF16/FP16 values each; 0: once per contraction term)."""
         _capi.check(self._lib.sdt_job_set_mixed_segment(self._h, int(chunks)), "sdt_job_set_mixed_segment")
 
+    def set_max_ctas(self, sms: int, sm_exclusive: bool = False) -> None:
+        """Cap the persistent launches at `sms` SMs' worth of CTAs (0: all);
+        with sm_exclusive the FP64 launches take one CTA per SM, so a capped
+        launch occupies exactly `sms` SMs."""
+        _capi.check(self._lib.sdt_job_set_max_ctas(self._h, int(sms)), "sdt_job_set_max_ctas")
+        _capi.check(self._lib.sdt_job_set_sm_exclusive(self._h, 1 if sm_exclusive else 0), "sdt_job_set_sm_exclusive")
+
     def set_mixed_cluster(self, ctas: int) -> None:
         """Mixed form: clusters of 1 (default) or 4 CTAs sharing operand tiles."""
         _capi.check(self._lib.sdt_job_set_mixed_cluster(self._h, int(ctas)), "sdt_job_set_mixed_cluster")

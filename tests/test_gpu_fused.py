@@ -103,6 +103,21 @@ def test_fused_deterministic(gpu):
     assert a[0] == b[0] and a[1] == b[1] and np.array_equal(a[2], b[2])
 
 
+def test_fused_capped_launches_same_bits(gpu):
+    """Results do not depend on the launch width: capped persistent launches,
+    with and without one CTA per SM, give the bits of the full launch."""
+    t = ng.Tiling([3, 5, 2], [4, 6, 4, 3]).with_evl(2)
+    files = ng.synth_inputs(t, 2)
+    kl = ng.task_list(t)
+    with ng.TriplesJob(t) as job:
+        job.load(*files)
+        ref = job.run(kl, per_task=True)
+        for sms, excl in ((8, False), (8, True), (1, True)):
+            job.set_max_ctas(sms, sm_exclusive=excl)
+            e = job.run(kl, per_task=True)
+            assert e[0] == ref[0] and e[1] == ref[1] and np.array_equal(e[2], ref[2]), (sms, excl)
+
+
 def test_fused_subsets_add_up(gpu):
     """Energies are additive over tuple ranges (the sharding contract)."""
     t = ng.Tiling([3, 5, 2], [4, 6, 4, 3]).with_evl(2)

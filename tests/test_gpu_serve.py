@@ -50,3 +50,19 @@ def test_job_over_budget_is_refused(cuda_device):
         srv.drain(60)
         x = srv.status(tk)
     assert x["state"] == -1 and x["rc"] == 3 and "budget" in x["msg"]
+
+
+def test_fp64_check_waits_for_admissible_jobs(cuda_device):
+    """A checked job delivers its energies first (state 3), the jobs queued
+    behind it run next, and its FP64 check runs when none is waiting."""
+    specs = serve.job_stream(3, 100.0, 5, 16, 16)  # jobs of some ms: all three are queued before the first ends
+    files = serve.prepare(specs)
+    prec = ng.PREC_MIXED_FP16
+    with serve.Server(40 << 30, slots=1) as srv:
+        tickets = [srv.submit(s.tiling, f, prec, check_fp64=(s.id == 0)) for s, f in zip(specs, files)]
+        srv.drain(600)
+        st = [srv.status(t) for t in tickets]
+    assert all(x["state"] == 2 for x in st), [x["msg"] for x in st]
+    assert st[0]["ran"] <= st[1]["admitted"] and st[2]["ran"] <= st[0]["finished"]
+    mixed, fp64 = _alone(specs[0], files[0], prec)
+    assert st[0]["energy"] == mixed and st[0]["fp64"] == fp64
