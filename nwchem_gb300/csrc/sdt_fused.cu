@@ -712,42 +712,44 @@ extern "C" int sdt_job_load(sdt_job *j, const sdt_file *f1, const sdt_file *f2,
     // (one launch per 65535 copy jobs), which need SMs.
     const sdt_file *files[3] = {f1, f2, fv};
     double *raw[3] = {nullptr, nullptr, nullptr};
+    CopyJob *jobs_d = nullptr;
+    // On an error: let issued work finish, return every buffer, leave the
+    // job unloaded.
+    auto bail = [&](int code) {
+        cudaStreamSynchronize(st);
+        for (int f = 0; f < 3; ++f) gpu_put(raw[f]);
+        gpu_put(jobs_d);
+        job_free_arrays(j);
+        return code;
+    };
     int rc = SDT_OK;
     for (int f = 0; f < 3; ++f) {
         raw[f] = (double *)gpu_get((size_t)std::max<int64_t>(files[f]->ndata, 1) * sizeof(double));
-        if (!raw[f]) {
-            for (int g = 0; g < f; ++g) gpu_put(raw[g]);
-            return fail(SDT_ERR_NOMEM, "sdt_job_load: raw file allocation");
-        }
+        if (!raw[f]) return bail(fail(SDT_ERR_NOMEM, "sdt_job_load: raw file allocation"));
         if (files[f]->ndata > 0) {
             touch_host_pages(files[f]->data, (size_t)files[f]->ndata * sizeof(double));
             rc = cuda_check(cudaMemcpyAsync(raw[f], files[f]->data, (size_t)files[f]->ndata * sizeof(double),
                                             cudaMemcpyHostToDevice, st), "sdt_job_load");
-            if (rc) return rc;
+            if (rc) return bail(rc);
         }
         tr.mark(f == 0 ? "file T1" : f == 1 ? "file T2" : "file V2", st);
     }
     for (int a = 0; a < DST_N; ++a) {
         j->arr[a] = (double *)gpu_get(want[a] * sizeof(double));
-        if (!j->arr[a]) {
-            cudaStreamSynchronize(st);
-            for (int f = 0; f < 3; ++f) gpu_put(raw[f]);
-            job_free_arrays(j);
-            return fail(SDT_ERR_NOMEM, "sdt_job_load: dense operand allocation");
-        }
+        if (!j->arr[a]) return bail(fail(SDT_ERR_NOMEM, "sdt_job_load: dense operand allocation"));
         j->arr_n[a] = want[a];
         rc = cuda_check(cudaMemsetAsync(j->arr[a], 0, want[a] * sizeof(double), st), "sdt_job_load");
-        if (rc) return rc;
+        if (rc) return bail(rc);
     }
     rc = cuda_check(cudaMemcpyAsync(j->pair_off, pair.data(), pair.size() * sizeof(int64_t),
                                     cudaMemcpyHostToDevice, st), "sdt_job_load");
-    if (rc) return rc;
+    if (rc) return bail(rc);
     tr.mark("allocate+clear", st);
-    CopyJob *jobs_d = (CopyJob *)gpu_get(std::max<size_t>(jobs.size(), 1) * sizeof(CopyJob));
-    if (!jobs_d) return fail(SDT_ERR_NOMEM, "sdt_job_load: job list");
+    jobs_d = (CopyJob *)gpu_get(std::max<size_t>(jobs.size(), 1) * sizeof(CopyJob));
+    if (!jobs_d) return bail(fail(SDT_ERR_NOMEM, "sdt_job_load: job list"));
     rc = cuda_check(cudaMemcpyAsync(jobs_d, jobs.data(), jobs.size() * sizeof(CopyJob),
                                     cudaMemcpyHostToDevice, st), "sdt_job_load");
-    if (rc) return rc;
+    if (rc) return bail(rc);
     IngestArgs g;
     for (int f = 0; f < 3; ++f) g.src[f] = raw[f];
     for (int a = 0; a < DST_N; ++a) g.dst[a] = j->arr[a];
@@ -758,14 +760,13 @@ extern "C" int sdt_job_load(sdt_job *j, const sdt_file *f1, const sdt_file *f2,
         count_launch();
     }
     rc = cuda_check(cudaGetLastError(), "sdt_job_load: ingest");
+    if (rc) return bail(rc);
     // The raw copies and the job list are released once the stream is done.
-    cudaError_t e = cudaStreamSynchronize(st);
+    rc = cuda_check(cudaStreamSynchronize(st), "sdt_job_load: ingest");
     tr.mark("ingest", nullptr);
+    if (rc) return bail(rc);
     for (int f = 0; f < 3; ++f) gpu_put(raw[f]);
     gpu_put(jobs_d);
-    if (rc) return rc;
-    rc = cuda_check(e, "sdt_job_load: ingest");
-    if (rc) return rc;
     j->loaded = true;
     return SDT_OK;
 }
