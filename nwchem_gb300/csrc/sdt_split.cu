@@ -43,10 +43,13 @@
 // it while the energy warps evaluate the copy: the s1 products in FP32 from
 // FP32 copies of T1 and the vvoo block, then, in FP64, the denominator, the
 // division and the two energy sums.  So the energy work of one item overlaps
-// the contractions of the next.
+// the contractions of the next.  In the tensor-memory hold variant (HOLD = 1)
+// the last drain writes the finished sub-box into the upper 256 TMEM columns
+// instead, one accumulator remains, and 16 energy warps read the sub-box
+// from TMEM.
 //
 // Warp roles: 0 TMA producer, 1 MMA issuer + TMEM owner, 2-3 idle, 4-7 drain
-// (TMEM lane quadrant warp % 4), 8-15 energy.  Every mbarrier wait is bounded
+// (TMEM lane quadrant warp % 4), 8-15 energy (8-23 with HOLD = 1).  Every mbarrier wait is bounded
 // (2 s); on a timeout the kernel sets an error flag, lets issued copies and
 // MMAs land, frees TMEM and returns.
 #include "sdt_common.cuh"
@@ -68,6 +71,15 @@ constexpr uint64_t kWaitNs = 2000000000ull;  // 2 s per wait
 constexpr int SX_THREADS = 512;
 constexpr int SX_DRAIN = 128;                 // drain threads (warps 4-7)
 constexpr int SX_EPI = 256;                   // energy threads (warps 8-15)
+// Tensor-memory hold (the finished sub-box in TMEM, not in the energy warps'
+// registers): 768 threads, 16 energy warps (warps 8-23, four per SM
+// sub-partition, each a lane quadrant and a quarter of the hold columns).
+// The launch gives 80 registers per thread (65536 / 768, rounded down to 8);
+// warps 0-3 drop to 56, the drains to 72, the energy warps rise to 88:
+// 128*56 + 128*72 + 512*88 = 61440 = 768*80, and per sub-partition
+// (56 + 72 + 4*88)*32 = 15360 <= 16384.
+constexpr int SX_THREADS_H = 768, SX_EPI_H = 512;
+constexpr int SX_REG_LAUNCH_H = 80, SX_REG_HIGH_H = 88;
 // Register split (setmaxnreg): the launch gives 128 per thread (4 warps per
 // SM sub-partition); warps 0-3 drop to 56, the drain warps to 72 and the
 // energy warps rise to 192: 128*56 + 128*72 + 256*192 = 65536 = 512*128, and
@@ -78,6 +90,14 @@ static_assert(128 * SX_REG_LOW + 128 * SX_REG_DRAIN + 256 * SX_REG_HIGH <= SX_TH
 // setmaxnreg.dec may only lower and setmaxnreg.inc only raise a warp's count.
 static_assert(SX_REG_LOW <= SX_REG_LAUNCH && SX_REG_DRAIN <= SX_REG_LAUNCH && SX_REG_HIGH >= SX_REG_LAUNCH,
               "setmaxnreg direction");
+static_assert(SX_REG_LAUNCH_H * SX_THREADS_H <= 65536 && SX_REG_LAUNCH_H % 8 == 0 &&
+                  (SX_REG_LAUNCH_H + 8) * SX_THREADS_H > 65536,
+              "hold variant: launch registers = the most 768 threads can have");
+static_assert(128 * SX_REG_LOW + 128 * SX_REG_DRAIN + SX_EPI_H * SX_REG_HIGH_H <= SX_THREADS_H * SX_REG_LAUNCH_H,
+              "hold variant: register split");
+static_assert(SX_REG_LOW <= SX_REG_LAUNCH_H && SX_REG_DRAIN <= SX_REG_LAUNCH_H && SX_REG_HIGH_H >= SX_REG_LAUNCH_H,
+              "hold variant: setmaxnreg direction");
+static_assert((SX_REG_LOW + SX_REG_DRAIN + 4 * SX_REG_HIGH_H) * 32 <= 16384, "hold variant: sub-partition registers");
 constexpr int SX_BV = 8, SX_BO = 4, SX_NX = 32768;
 constexpr int SX_NS = 4;                      // operand stages
 constexpr int SX_A = 128 * 32, SX_B = 256 * 32;
@@ -629,7 +649,8 @@ __device__ __forceinline__ void energy_chunk(const float (&R)[N], const EDesc &d
 // columns (th: this warp's lane quadrant, column 128*half), 4 columns (the
 // k values of one c) at a time in rolled loops: a small loop body, and
 // registers free for the FP64 work.  All lanes take part in every TMEM load.
-__device__ __forceinline__ void energy_tmem(uint32_t th, const EDesc &d, const SplitParams &p, int half, int b,
+template <int NA>
+__device__ __forceinline__ void energy_tmem(uint32_t th, const EDesc &d, const SplitParams &p, int part, int b,
                                             int i, int j, double &e1, double &est) {
     const bool row_ok = b < d.nv[1] && i < d.nv[3] && j < d.nv[4];
     const int op = p.op;
@@ -647,8 +668,8 @@ __device__ __forceinline__ void energy_tmem(uint32_t th, const EDesc &d, const S
     const float t1bi = row_ok ? __ldg(t1b + pi) : 0.f, t1bj = row_ok ? __ldg(t1b + pj) : 0.f;
     const float4 t1bk = row_ok ? ld4(t1b + pk0) : make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll 1
-    for (int A = 0; A < 4; ++A) {
-        const int a = 4 * half + A;
+    for (int A = 0; A < NA; ++A) {
+        const int a = NA * part + A;
         const bool ok_a = row_ok && a < d.nv[0];
         const int ga = d.g[0] + a;
         const float *__restrict__ t1a = p.T1f + (int64_t)(ok_a ? ga : 0) * op;
@@ -703,17 +724,29 @@ __device__ __forceinline__ void energy_tmem(uint32_t th, const EDesc &d, const S
 }
 
 // Per-item pair: E[T] part f/S^2 sum X^2/D, E(T) part that + f/S sum X X_s/D.
-__device__ __forceinline__ void write_partial(double &e1, double &est, double *red, const EDesc &d,
-                                              const SplitParams &p, int ew, int lane, bool leader) {
-    const double x = warp_sum(e1), y = warp_sum(est);
-    if (lane == 0) {
-        red[2 * ew] = x;
-        red[2 * ew + 1] = y;
+// The sums run over 16 slots in a fixed order, slot = 4*quarter + quadrant
+// (quarter: a pair of a values, quadrant: the TMEM lane quadrant), whatever
+// the warp layout: NQ quarter partials per thread, the first quarter0 --
+// so both work-unit shapes give the same bits.
+template <int EPI, int NQ>
+__device__ __forceinline__ void write_partial(double (&e1)[NQ], double (&est)[NQ], double *red, const EDesc &d,
+                                              const SplitParams &p, int quarter0, int quadrant, int lane,
+                                              bool leader) {
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) {
+        const double x = warp_sum(e1[q]), y = warp_sum(est[q]);
+        if (lane == 0) {
+            const int slot = 4 * (quarter0 + q) + quadrant;
+            red[2 * slot] = x;
+            red[2 * slot + 1] = y;
+        }
+        e1[q] = 0.0;
+        est[q] = 0.0;
     }
-    named_bar(2, SX_EPI);
+    named_bar(2, EPI);
     if (leader) {
         double s1 = 0.0, s2 = 0.0;
-        for (int w = 0; w < SX_EPI / 32; ++w) {
+        for (int w = 0; w < 16; ++w) {
             s1 += red[2 * w];
             s2 += red[2 * w + 1];
         }
@@ -721,8 +754,6 @@ __device__ __forceinline__ void write_partial(double &e1, double &est, double *r
         p.part[2 * d.item] = et;
         p.part[2 * d.item + 1] = et + d.factor * s2 * p.inv_s;
     }
-    e1 = 0.0;
-    est = 0.0;
 }
 
 // HOLD = 0: the energy warps keep the finished sub-box in registers, two
@@ -730,8 +761,11 @@ __device__ __forceinline__ void write_partial(double &e1, double &est, double *r
 // TMEM columns, which the energy warps read 32 columns at a time (their
 // registers stay free for the FP64 work), one accumulator.
 template <int TYPE, int CS, int HOLD>
-__global__ void __launch_bounds__(SX_THREADS, 1) split_fused_kernel(const __grid_constant__ SplitParams p) {
+__global__ void __launch_bounds__(HOLD ? SX_THREADS_H : SX_THREADS, 1)
+    split_fused_kernel(const __grid_constant__ SplitParams p) {
     static_assert(HOLD == 0 || CS == 1, "tensor-memory hold with single CTAs only");
+    constexpr int EPI = HOLD ? SX_EPI_H : SX_EPI;   // energy threads
+    constexpr int NA = HOLD ? 2 : 4;                // a values per energy thread
     constexpr int PJ = CS == 4 ? 2 : 1;
     constexpr int NB = HOLD ? 1 : 2;
     extern __shared__ __align__(1024) uint8_t smem_raw[];
@@ -751,7 +785,7 @@ __global__ void __launch_bounds__(SX_THREADS, 1) split_fused_kernel(const __grid
     volatile int64_t *en_unit = (volatile int64_t *)(misc + 216);
     int *dr_nk = (int *)(misc + 224);              // [9] kept K chunks per term of the drained item
     EDesc *desc = (EDesc *)(misc + 320);
-    double *red = (double *)(misc + 512);          // [8 energy warps][2]
+    double *red = (double *)(misc + 512);          // [16 energy warps at most][2]
     const UnitRing ring{(int64_t *)(misc + 768), ufull, uempty};
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     constexpr int KE = TYPE == TM_F32 ? 8 : 16;
@@ -877,14 +911,18 @@ __global__ void __launch_bounds__(SX_THREADS, 1) split_fused_kernel(const __grid
         }
     } else {
         // ---------------- energy warps ----------------
-        asm volatile("setmaxnreg.inc.sync.aligned.u32 %0;" ::"n"(SX_REG_HIGH));
+        asm volatile("setmaxnreg.inc.sync.aligned.u32 %0;" ::"n"(HOLD ? SX_REG_HIGH_H : SX_REG_HIGH));
         const int et = threadIdx.x - 256;
-        const int mm = et & 127, half = et >> 7;
+        const int mm = et & 127, half = et >> 7;  // half: the part of the a range (a = NA*half + A)
         const int rb = mm >> 4, ri = (mm >> 2) & 3, rj_ = mm & 3;  // thread row (b;i,j)
         const int ew = et >> 5;
         const bool leader = (et == 0);
         float R[HOLD ? 1 : 128];
-        double e1 = 0.0, est = 0.0;
+        constexpr int NQ = HOLD ? 1 : 2;  // quarter partials per thread
+        double e1[NQ], est[NQ];
+#pragma unroll
+        for (int q = 0; q < NQ; ++q) e1[q] = est[q] = 0.0;
+        const int quarter0 = HOLD ? half : 2 * half;
         for (int n = 0;; ++n) {
             if (leader) {
                 int64_t si = CS == 1 ? ring_take(ring, n, abort) : unit0 + (int64_t)n * ustep;
@@ -912,18 +950,18 @@ __global__ void __launch_bounds__(SX_THREADS, 1) split_fused_kernel(const __grid
                 }
                 *en_unit = si;
             }
-            named_bar(2, SX_EPI);
+            named_bar(2, EPI);
             if (*en_unit < 0) break;
             const EDesc &d = *desc;
             if constexpr (HOLD) {
-                // the sub-box is in the hold columns: this warp's lane quadrant, columns 128*half + 32*A
+                // the sub-box is in the hold columns: this warp's lane quadrant, columns 32*(NA*half + A)
                 tc::tc_fence_after();
-                const uint32_t th = tmem + ((uint32_t)((warp & 3) * 32) << 16) + 256u + (uint32_t)(128 * half);
-                if (d.item >= 0) energy_tmem(th, d, p, half, rb, ri, rj_, e1, est);
+                const uint32_t th = tmem + ((uint32_t)((warp & 3) * 32) << 16) + 256u + (uint32_t)(32 * NA * half);
+                if (d.item >= 0) energy_tmem<NA>(th, d, p, half, rb, ri, rj_, e1[0], est[0]);
                 tc::tc_fence_before();
-                named_bar(2, SX_EPI);
+                named_bar(2, EPI);
                 if (leader) tc::mbar_arrive(xfree);  // the hold columns are free
-                if (d.item >= 0) write_partial(e1, est, red, d, p, ew, lane, leader);
+                if (d.item >= 0) write_partial<EPI, NQ>(e1, est, red, d, p, quarter0, warp & 3, lane, leader);
             } else {
 #pragma unroll
                 for (int A = 0; A < 4; ++A)
@@ -931,14 +969,14 @@ __global__ void __launch_bounds__(SX_THREADS, 1) split_fused_kernel(const __grid
                     for (int c = 0; c < 8; ++c)
 #pragma unroll
                         for (int k = 0; k < 4; ++k) R[A * 32 + c * 4 + k] = X[xaddr(4 * half + A, rb, c, ri, rj_, k)];
-                named_bar(2, SX_EPI);
+                named_bar(2, EPI);
                 if (leader) tc::mbar_arrive(xfree);
                 if (d.item >= 0) {  // a box outside the tuple has no item
-                    energy_chunk<0, 0, 128>(R, d, p, half, rb, ri, rj_, e1, est);
-                    energy_chunk<1, 32, 128>(R, d, p, half, rb, ri, rj_, e1, est);
-                    energy_chunk<2, 64, 128>(R, d, p, half, rb, ri, rj_, e1, est);
-                    energy_chunk<3, 96, 128>(R, d, p, half, rb, ri, rj_, e1, est);
-                    write_partial(e1, est, red, d, p, ew, lane, leader);
+                    energy_chunk<0, 0, 128>(R, d, p, half, rb, ri, rj_, e1[0], est[0]);
+                    energy_chunk<1, 32, 128>(R, d, p, half, rb, ri, rj_, e1[0], est[0]);
+                    energy_chunk<2, 64, 128>(R, d, p, half, rb, ri, rj_, e1[NQ - 1], est[NQ - 1]);
+                    energy_chunk<3, 96, 128>(R, d, p, half, rb, ri, rj_, e1[NQ - 1], est[NQ - 1]);
+                    write_partial<EPI, NQ>(e1, est, red, d, p, quarter0, warp & 3, lane, leader);
                 }
             }
         }
@@ -1391,7 +1429,7 @@ int mixed_launch(sdt_job *j, const LaunchArgs &a, cudaStream_t st) {
         attr[0].val.clusterDim.y = 1;
         attr[0].val.clusterDim.z = 1;
         cudaLaunchConfig_t cfg = {};
-        cfg.blockDim = dim3(SX_THREADS);
+        cfg.blockDim = dim3(a.cluster == 2 ? SX_THREADS_H : SX_THREADS);
         cfg.dynamicSmemBytes = SX_SMEM_ALLOC;
         cfg.stream = st;
         cfg.gridDim = dim3((unsigned)a.grid);
