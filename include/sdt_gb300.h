@@ -295,6 +295,10 @@ int sdt_server_status(sdt_server *server, int64_t ticket, int *state,
 /* CTAs of each deferred FP64 check (default a quarter of the SMs); while a
  * check runs, mixed jobs launch on the remaining SMs.  0: no cap. */
 int sdt_server_set_check_ctas(sdt_server *server, int ctas);
+/* Cancels a queued job (state -1, SDT_ERR_STATE); an admitted job is not
+ * stopped (SDT_ERR_STATE is returned). */
+int sdt_server_cancel(sdt_server *server, int64_t ticket);
+/* Waits for every submitted job (SDT_ERR_TIMEOUT after timeout_s). */
 int sdt_server_drain(sdt_server *server, double timeout_s);
 int64_t sdt_server_peak_bytes(sdt_server *server);
 int sdt_server_destroy(sdt_server *server);
@@ -349,6 +353,11 @@ int sdt_tc_selftest16(const void *a_hi, const void *a_lo, const void *b_hi,
  * reference counterpart): largest relative difference from the IEEE
  * quotient over n seeded (numerator, denominator) pairs. */
 int sdt_check_division(int64_t n, uint64_t seed, double *max_rel_err);
+/* Failure-path check (no reference counterpart): one bounded device wait on
+ * an mbarrier nothing arrives on, limited to timeout_s (0 < timeout_s <= 1).
+ * Returns SDT_ERR_TIMEOUT with *waited_s the time waited; the CUDA context
+ * stays usable. */
+int sdt_check_wait_timeout(double timeout_s, double *waited_s);
 
 #ifdef __cplusplus
 }

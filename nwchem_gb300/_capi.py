@@ -73,6 +73,7 @@ def _declare(lib):
         "sdt_server_status": (C.c_int, [C.c_void_p, C.c_int64, C.POINTER(C.c_int), PD, PD, PD, C.c_char_p,
                                         C.c_size_t]),
         "sdt_server_drain": (C.c_int, [C.c_void_p, C.c_double]),
+        "sdt_server_cancel": (C.c_int, [C.c_void_p, C.c_int64]),
         "sdt_server_set_check_ctas": (C.c_int, [C.c_void_p, C.c_int]),
         "sdt_job_set_sm_exclusive": (C.c_int, [C.c_void_p, C.c_int]),
         "sdt_server_peak_bytes": (C.c_int64, [C.c_void_p]),
@@ -85,6 +86,7 @@ def _declare(lib):
         "sdt_tc_selftest16": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int,
                                         C.c_void_p]),
         "sdt_check_division": (C.c_int, [C.c_int64, C.c_uint64, C.POINTER(C.c_double)]),
+        "sdt_check_wait_timeout": (C.c_int, [C.c_double, C.POINTER(C.c_double)]),
         "compute_en_": (None, [PD, PD, PD, PD, PD, PD, PD, PD, PI64, PI64, PI64, PI64, PI64, PI64, PD, PD]),
         "dev_mem_d_": (None, [PI64] * 6),
         "dev_mem_s_": (None, [PI64] * 6),

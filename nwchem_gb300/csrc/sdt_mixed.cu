@@ -267,6 +267,27 @@ __global__ void division_check_kernel(int64_t n, uint64_t seed, unsigned long lo
     atomicMax(worst_bits, (unsigned long long)__double_as_longlong(worst));
 }
 
+// The bounded mbarrier wait every kernel of the library uses, on a barrier
+// nothing arrives on: it must give up after timeout_ns and report it.
+// out[0] = SDT_ERR_TIMEOUT when it gave up (0 if the barrier completed),
+// out[1] = microseconds waited.
+__global__ void wait_timeout_kernel(uint64_t timeout_ns, int *out) {
+    __shared__ uint64_t bar;
+    __shared__ int abort_flag;
+    if (threadIdx.x == 0) {
+        tc::mbar_init(&bar, 1);
+        abort_flag = 0;
+        tc::fence_mbar_init();
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const uint64_t t0 = tc::global_ns();
+        const bool ok = tc::mbar_wait(&bar, 0, timeout_ns, &abort_flag);  // phase 0 never completes
+        out[0] = ok ? 0 : SDT_ERR_TIMEOUT;
+        out[1] = (int)((tc::global_ns() - t0) / 1000);
+    }
+}
+
 }  // namespace
 }  // namespace sdt
 
@@ -308,4 +329,30 @@ extern "C" int sdt_check_division(int64_t n, uint64_t seed, double *max_rel_err)
     if (rc) return rc;
     std::memcpy(max_rel_err, &h, sizeof(double));
     return SDT_OK;
+}
+
+// Failure-path check (no reference counterpart): one bounded wait on an
+// mbarrier nothing arrives on, limited to timeout_s (at most 1 s).  Returns
+// SDT_ERR_TIMEOUT with *waited_s the time it waited, as a kernel whose wait
+// ran out would; the context stays usable.
+extern "C" int sdt_check_wait_timeout(double timeout_s, double *waited_s) {
+    if (!(timeout_s > 0.0 && timeout_s <= 1.0) || !waited_s)
+        return fail(SDT_ERR_ARG, "sdt_check_wait_timeout: timeout must be in (0, 1] s");
+    int *d = (int *)gpu_get(2 * sizeof(int));
+    if (!d) return fail(SDT_ERR_NOMEM, "sdt_check_wait_timeout");
+    cudaStream_t st = lib_stream();
+    int h[2] = {0, 0};
+    int rc = cuda_check(cudaMemsetAsync(d, 0, 2 * sizeof(int), st), "sdt_check_wait_timeout");
+    if (!rc) {
+        wait_timeout_kernel<<<1, 32, 0, st>>>((uint64_t)(timeout_s * 1e9), d);
+        count_launch();
+        rc = cuda_check(cudaGetLastError(), "sdt_check_wait_timeout");
+    }
+    if (!rc) rc = cuda_check(cudaMemcpyAsync(h, d, sizeof(h), cudaMemcpyDeviceToHost, st), "sdt_check_wait_timeout");
+    if (!rc) rc = cuda_check(cudaStreamSynchronize(st), "sdt_check_wait_timeout");
+    gpu_put(d);
+    if (rc) return rc;
+    *waited_s = h[1] * 1e-6;
+    if (h[0] == SDT_ERR_TIMEOUT) return fail(SDT_ERR_TIMEOUT, "sdt_check_wait_timeout: the bounded wait ran out");
+    return h[0];
 }

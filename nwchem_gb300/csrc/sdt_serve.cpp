@@ -382,6 +382,25 @@ extern "C" int sdt_server_status(sdt_server *s, int64_t ticket, int *state, doub
     return j.state < 0 ? j.err : SDT_OK;
 }
 
+// Cancels a job that is still queued: it leaves the queue with state -1 and
+// SDT_ERR_STATE ("cancelled").  A job already admitted runs to the end
+// (SDT_ERR_STATE is returned and nothing changes).
+extern "C" int sdt_server_cancel(sdt_server *s, int64_t ticket) {
+    if (!s) return fail(SDT_ERR_ARG, "sdt_server_cancel: null server");
+    std::lock_guard<std::mutex> lk(s->mu);
+    if (ticket < 0 || ticket >= (int64_t)s->jobs.size()) return fail(SDT_ERR_ARG, "sdt_server_cancel: bad ticket");
+    sdt_server::Job *job = s->jobs[ticket].get();
+    auto it = std::find(s->queue.begin(), s->queue.end(), job);
+    if (it == s->queue.end()) return fail(SDT_ERR_STATE, "sdt_server_cancel: the job is no longer queued");
+    s->queue.erase(it);
+    job->state = -1;
+    job->err = SDT_ERR_STATE;
+    job->msg = "sdt_server: cancelled while queued";
+    job->t_start = job->t_end = s->now();
+    s->cv.notify_all();
+    return SDT_OK;
+}
+
 // Waits until every submitted job has finished (or timeout_s passed:
 // SDT_ERR_TIMEOUT).
 extern "C" int sdt_server_drain(sdt_server *s, double timeout_s) {

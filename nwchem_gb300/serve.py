@@ -116,6 +116,10 @@ class Server:
                 "ran": float(tm[3]), "finished": float(tm[4]),
                 "msg": buf.value.decode(errors="replace")}
 
+    def cancel(self, ticket: int) -> None:
+        """Cancel a job that is still queued (raises SdtError if it was admitted)."""
+        _capi.check(self._lib.sdt_server_cancel(self._h, int(ticket)), "sdt_server_cancel")
+
     def drain(self, timeout: float = 3600.0) -> None:
         _capi.check(self._lib.sdt_server_drain(self._h, float(timeout)), "sdt_server_drain")
 
