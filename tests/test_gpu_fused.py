@@ -33,6 +33,7 @@ TILINGS = [
     ([8, 12], [20, 24], None, None),               # multiples of 4
     ([3, 2, 3], [4, 5, 4, 3], [0, 1, 1], [1, 0, 1, 0]),   # irreps: filtered h7b/p7b
     ([4, 4, 4, 4], [8, 8, 8, 8], [0, 1, 2, 3], [3, 2, 1, 0]),
+    ([1, 2, 3, 4, 5], [5, 4, 3, 2, 1], None, None),  # every tile size 1..5 in every position
 ]
 
 

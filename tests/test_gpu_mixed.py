@@ -93,6 +93,7 @@ MIXED_TILINGS = [
     ([3, 5, 2], [9, 6, 10, 3], None, None),
     ([8, 12], [16, 24], None, None),               # whole boxes
     ([3, 2, 3], [4, 5, 4, 3], [0, 1, 1], [1, 0, 1, 0]),   # irreps
+    ([1, 2, 3, 4, 5], [9, 7, 3, 1, 2], None, None),          # tiny and ragged tiles in every position
 ]
 
 
