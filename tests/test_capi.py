@@ -89,3 +89,17 @@ def test_synth_file_layout():
         assert offs[0] == 0 and (np.diff(offs) > 0).all()
         assert f.lookup(int(keys[-1])) == int(offs[-1])
         assert f.lookup(-5) == -1
+
+
+def test_task_list_writes_only_its_rows():
+    """Canary-padded output: sdt_tasks_list fills exactly 7 * n int64 values."""
+    t = ng.Tiling([3, 5, 2], [4, 6, 4, 3], occ_sym=[0, 1, 1], vir_sym=[1, 0, 1, 0])
+    lib = _capi.lib()
+    ts = t.struct()
+    n = lib.sdt_tasks_count(C.byref(ts))
+    assert n > 0
+    canary = np.int64(-0x5A5A5A5A5A5A5A5B)
+    buf = np.full(7 * n + 64, canary, dtype=np.int64)
+    assert lib.sdt_tasks_list(C.byref(ts), n, buf.ctypes.data_as(_capi.PI64)) == 0
+    assert np.all(buf[7 * n:] == canary)
+    assert np.array_equal(buf[:7 * n].reshape(n, 7), ng.task_list(t))

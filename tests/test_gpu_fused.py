@@ -237,3 +237,33 @@ def test_restricted_tiling_both_forms(gpu):
     assert g1 == pytest.approx(e1, rel=REL, abs=0) and g2 == pytest.approx(e2, rel=REL, abs=0)
     assert np.abs(gpt - pt).max() <= REL * max(abs(e1), abs(e2))
     assert m1 == pytest.approx(e1, rel=2e-6) and m2 == pytest.approx(e2, rel=2e-6)
+
+
+def test_per_tuple_output_writes_only_its_pairs(gpu):
+    """Canary-padded outputs of a one-shot run and of a plan: exactly 2 * n
+    doubles are written, and the energies out[2] only."""
+    import ctypes as C
+    t = ng.Tiling([3, 5, 2], [4, 6, 4, 3]).with_evl(2)
+    files = ng.synth_inputs(t, 2)
+    kl = np.ascontiguousarray(ng.task_list(t))
+    n = len(kl)
+    lib = _capi.lib()
+    with ng.TriplesJob(t) as job:
+        job.load(*files)
+        ref = job.run(kl, per_task=True)
+        for prec in (ng.PREC_FP64, ng.PREC_MIXED_FP16):
+            pt = np.full(2 * n + 32, np.nan)
+            e = np.full(2 + 8, np.nan)
+            rc = lib.sdt_job_run(job._h, kl.ctypes.data_as(_capi.PI64), n, prec, e.ctypes.data_as(_capi.PD),
+                                 pt.ctypes.data_as(_capi.PD), None)
+            assert rc == 0
+            assert np.all(np.isnan(pt[2 * n:])) and np.all(np.isnan(e[2:]))
+            assert not np.any(np.isnan(pt[:2 * n])) and not np.any(np.isnan(e[:2]))
+            if prec == ng.PREC_FP64:
+                assert np.array_equal(pt[:2 * n].reshape(n, 2), ref[2]) and (e[0], e[1]) == ref[:2]
+        with ng.Plan(job, kl, ng.PREC_FP64) as p:
+            pt = np.full(2 * n + 32, np.nan)
+            e = np.full(2 + 8, np.nan)
+            assert lib.sdt_plan_run(p._h, None, e.ctypes.data_as(_capi.PD), pt.ctypes.data_as(_capi.PD)) == 0
+            assert np.all(np.isnan(pt[2 * n:])) and np.all(np.isnan(e[2:]))
+            assert np.array_equal(pt[:2 * n].reshape(n, 2), ref[2])
