@@ -397,6 +397,39 @@ def _measured_bf16() -> tuple[float, str]:
         return 1900.0, "fallback 1.9 PFLOP/s bf16 (no MEASURED_PEAKS.json)"
 
 
+def workload_o10v40(args) -> None:
+    """o=10, v=40, one tile each, seed 0 (one tuple, 5.875e10 FLOPs): the FP64
+    form and each mixed form on the GPU (kernel time, average of 5 runs after
+    a warm-up), the oracle on all host cores over the whole problem, and each
+    result against the oracle's energies."""
+    import torch
+
+    import nwchem_gb300 as ng
+    from oracle import oracle as orc
+    torch.cuda.set_device(0)
+    t = ng.config_tiling(0)
+    kl = ng.task_list(t)
+    files = ng.synth_inputs(t, 0)
+    fl = ng.flops(t, kl)
+    t0 = time.perf_counter()
+    o1, o2, _, _ = orc.Problem(t, *files).ccsd_t()
+    cpu_s = time.perf_counter() - t0
+    out = {"workload": "o10v40: o=10, v=40, one tile each, seed 0", "tuples": int(len(kl)), "flops": fl,
+           "oracle": {"E": [o1, o2], "s": cpu_s, "tflops": fl / cpu_s / 1e12, "cores": os.cpu_count()}}
+    with ng.TriplesJob(t) as job:
+        job.load(*files)
+        job.set_timing(True)
+        for form, prec in [("fp64", ng.PREC_FP64)] + list(MIXED_FORMS):
+            e = job.run(kl, precision=prec)
+            ms = []
+            for _ in range(5):
+                e = job.run(kl, precision=prec)
+                ms.append(job.last_kernel_ms)
+            out[form] = {"E": list(e), "kernel_ms": float(np.mean(ms)), "tflops": fl / np.mean(ms) / 1e9,
+                         "rel_err_E(T)": (e[1] - o2) / abs(o2), "rel_err_E[T]": (e[0] - o1) / abs(o1)}
+    print(json.dumps(out), flush=True)
+
+
 def workload_o64v512(args) -> None:
     """o=64 (2x32), v=512 (8x64), seed 2: each mixed form over a strided tenth
     of the 480-tuple list, and every form plus FP64 on one tuple for the error."""
@@ -574,7 +607,7 @@ def main() -> None:
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--profile", action="store_true", help="small single-launch case for ncu")
     ap.add_argument("--tuples", type=int, default=2, help="tuples in the --profile case")
-    ap.add_argument("--workload", default="o40v300", choices=["o40v300", "o64v512", "sym8", "serve"])
+    ap.add_argument("--workload", default="o40v300", choices=["o40v300", "o10v40", "o64v512", "sym8", "serve"])
     ap.add_argument("--jobs", type=int, default=200, help="serve: jobs in the stream")
     ap.add_argument("--rate", type=float, default=50.0, help="serve: Poisson arrival rate (jobs/s)")
     ap.add_argument("--omin", type=int, default=8, help="serve: smallest occupied size")
@@ -592,7 +625,9 @@ def main() -> None:
         ap.error("--warmup must be at least 3")
     import nwchem_gb300.build as b
     b.build()
-    if args.workload == "o64v512":
+    if args.workload == "o10v40":
+        workload_o10v40(args)
+    elif args.workload == "o64v512":
         workload_o64v512(args)
     elif args.workload == "sym8":
         workload_sym8(args)
