@@ -312,6 +312,15 @@ int sdt_admission_simulate(int64_t n, const double *arrival,
                            const int64_t *bytes, const double *service,
                            int64_t budget, int slots, double *start,
                            double *end);
+/* The serving policy with deferred FP64 checks, simulated on the host: as
+ * sdt_admission_simulate, plus check_service[q] (< 0: no check); a pending
+ * check takes a free slot only when no queue head can be admitted, and the
+ * job's bytes stay admitted until its check ends.  start, ready (energies)
+ * and done (check finished) receive the times (-1: refused). */
+int sdt_serving_simulate(int64_t n, const double *arrival, const int64_t *bytes,
+                         const double *service, const double *check_service,
+                         int64_t budget, int slots, double *start,
+                         double *ready, double *done);
 /* Caps a job's persistent launches at `ctas` SMs' worth of CTAs (0: all
  * SMs; a mixed launch runs one CTA per SM, an FP64 launch up to four). */
 int sdt_job_set_max_ctas(sdt_job *job, int ctas);

@@ -80,6 +80,7 @@ def _declare(lib):
         "sdt_server_destroy": (C.c_int, [C.c_void_p]),
         "sdt_job_bytes": (C.c_int64, [C.POINTER(SdtTiling), C.c_int]),
         "sdt_admission_simulate": (C.c_int, [C.c_int64, PD, PI64, PD, C.c_int64, C.c_int, PD, PD]),
+        "sdt_serving_simulate": (C.c_int, [C.c_int64, PD, PI64, PD, PD, C.c_int64, C.c_int, PD, PD, PD]),
         "sdt_job_set_max_ctas": (C.c_int, [C.c_void_p, C.c_int]),
         "sdt_job_stream": (C.c_void_p, [C.c_void_p]),
         "sdt_tc_selftest": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]),

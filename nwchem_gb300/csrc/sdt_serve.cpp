@@ -488,3 +488,82 @@ extern "C" int sdt_admission_simulate(int64_t n, const double *arrival, const in
     }
     return SDT_OK;
 }
+
+// The serving policy with deferred FP64 checks, as an event simulation on the
+// host (the same rules as the workers above): jobs arrive at arrival[q]
+// (ascending) with device bytes bytes[q], mixed run time service[q] and FP64
+// check time check_service[q] (< 0: no check).  A queue head is refused if it
+// can never fit and admitted (FIFO) when a slot is free and its bytes fit;
+// only when no head can be admitted does a free slot take the oldest pending
+// check.  A checked job keeps its bytes, but not its slot, between its
+// energies and its check.  start[q], ready[q] (energies) and done[q] (check
+// finished, memory returned) receive the times; -1 for a refused job.
+extern "C" int sdt_serving_simulate(int64_t n, const double *arrival, const int64_t *bytes, const double *service,
+                                    const double *check_service, int64_t budget, int slots, double *start,
+                                    double *ready, double *done) {
+    if (n < 0 || (n > 0 && (!arrival || !bytes || !service || !check_service || !start || !ready || !done)) ||
+        budget <= 0 || slots < 1)
+        return fail(SDT_ERR_ARG, "sdt_serving_simulate: bad argument");
+    struct Run {
+        double end;
+        int64_t job;
+        bool check;
+    };
+    Admission adm;
+    adm.budget = budget;
+    adm.slots = slots;
+    std::vector<Run> running;
+    std::deque<int64_t> checks;
+    int64_t head = 0;
+    double clock = 0.0;
+    while (true) {
+        bool progress = true;
+        while (progress) {
+            progress = false;
+            const bool has_head = head < n && arrival[head] <= clock;
+            if (has_head && !adm.fits_ever(bytes[head])) {
+                start[head] = ready[head] = done[head] = -1.0;
+                ++head;
+                progress = true;
+            } else if (has_head && adm.can_admit(bytes[head])) {
+                adm.admit(bytes[head]);
+                start[head] = clock;
+                running.push_back({clock + service[head], head, false});
+                ++head;
+                progress = true;
+            } else if (!checks.empty() && adm.busy < adm.slots) {
+                adm.take_slot();
+                const int64_t q = checks.front();
+                checks.pop_front();
+                running.push_back({clock + check_service[q], q, true});
+                progress = true;
+            }
+        }
+        double next = 1e300;
+        for (const Run &r : running) next = std::min(next, r.end);
+        if (head < n && arrival[head] > clock) next = std::min(next, arrival[head]);
+        if (next >= 1e300) break;
+        clock = next;
+        for (size_t k = 0; k < running.size();) {
+            const Run r = running[k];
+            if (r.end > clock) {
+                ++k;
+                continue;
+            }
+            running[k] = running.back();
+            running.pop_back();
+            if (r.check) {
+                adm.release(bytes[r.job]);
+                done[r.job] = r.end;
+            } else if (check_service[r.job] >= 0.0) {
+                ready[r.job] = r.end;
+                adm.free_slot();  // the bytes stay admitted until the check
+                checks.push_back(r.job);
+            } else {
+                ready[r.job] = done[r.job] = r.end;
+                adm.release(bytes[r.job]);
+            }
+        }
+    }
+    return SDT_OK;
+}

@@ -41,6 +41,22 @@ def simulate(arrival, nbytes, service, budget: int, slots: int):
     return start, end
 
 
+def simulate_checks(arrival, nbytes, service, check_service, budget: int, slots: int):
+    """The server's policy with deferred FP64 checks on the host: (start,
+    ready, done) per job; check_service < 0 means no check."""
+    a = np.ascontiguousarray(arrival, dtype=np.float64)
+    b = np.ascontiguousarray(nbytes, dtype=np.int64)
+    s = np.ascontiguousarray(service, dtype=np.float64)
+    c = np.ascontiguousarray(check_service, dtype=np.float64)
+    start, ready, done = np.zeros(len(a)), np.zeros(len(a)), np.zeros(len(a))
+    P = _capi.PD
+    _capi.check(_capi.lib().sdt_serving_simulate(len(a), a.ctypes.data_as(P), b.ctypes.data_as(_capi.PI64),
+                                                 s.ctypes.data_as(P), c.ctypes.data_as(P), int(budget), int(slots),
+                                                 start.ctypes.data_as(P), ready.ctypes.data_as(P),
+                                                 done.ctypes.data_as(P)), "sdt_serving_simulate")
+    return start, ready, done
+
+
 def _split(total: int, sizes, rng) -> list[int]:
     out, left = [], total
     while left > 0:

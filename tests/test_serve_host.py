@@ -71,3 +71,74 @@ def test_job_stream_is_seeded_and_sized():
         assert set(t.occ[:-1]) <= set(serve.OCC_SIZES) and set(t.vir[:-1]) <= set(serve.VIR_SIZES)
     arr = np.array([s.arrival for s in a])
     assert np.all(np.diff(arr) > 0) and 0.2 < arr[-1] < 1.5   # ~30 jobs at 50/s
+
+
+def _check_deferred(arr, nb, svc, chk, budget, slots):
+    start, ready, done = serve.simulate_checks(arr, nb, svc, chk, budget, slots)
+    ok = start >= 0
+    assert np.array_equal(ok, nb <= budget)
+    assert np.all(start[ok] >= arr[ok] - 1e-12)
+    assert np.all(np.diff(start[ok]) >= -1e-12)                      # FIFO admission
+    assert np.allclose(ready[ok] - start[ok], svc[ok])
+    has = ok & (chk >= 0)
+    assert np.allclose(done[ok & (chk < 0)], ready[ok & (chk < 0)])
+    assert np.all(done[has] - ready[has] >= chk[has] - 1e-12)        # a check never starts before the energies
+    # at every event: slots hold mixed runs and running checks; admitted bytes (until done) fit
+    times = np.unique(np.concatenate([start[ok], ready[ok], done[ok]]))
+    for t in times:
+        mixed = ok & (start <= t + 1e-12) & (ready > t + 1e-12)
+        checking = has & (done - chk <= t + 1e-12) & (done > t + 1e-12)
+        assert mixed.sum() + checking.sum() <= slots
+        held = ok & (start <= t + 1e-12) & (done > t + 1e-12)
+        assert nb[held].sum() <= budget
+    return start, ready, done
+
+
+def test_deferred_checks_random_streams():
+    rng = np.random.default_rng(1)
+    for trial in range(25):
+        n = int(rng.integers(1, 50))
+        arr = np.cumsum(rng.exponential(0.02, n))
+        nb = rng.integers(1, 100, n).astype(np.int64)
+        svc = rng.uniform(0.001, 0.1, n)
+        chk = np.where(rng.random(n) < 0.3, rng.uniform(0.05, 2.0, n), -1.0)
+        budget, slots = int(rng.integers(100, 300)), int(rng.integers(1, 5))
+        nb[rng.random(n) < 0.05] = budget + 1
+        _check_deferred(arr, nb, svc, chk, budget, slots)
+
+
+def test_without_checks_matches_admission_policy():
+    rng = np.random.default_rng(2)
+    n = 40
+    arr = np.cumsum(rng.exponential(0.02, n))
+    nb = rng.integers(1, 100, n).astype(np.int64)
+    svc = rng.uniform(0.001, 0.2, n)
+    s0, e0 = serve.simulate(arr, nb, svc, 150, 3)
+    s1, r1, d1 = serve.simulate_checks(arr, nb, svc, np.full(n, -1.0), 150, 3)
+    assert np.allclose(s0, s1) and np.allclose(e0, r1) and np.allclose(r1, d1)
+
+
+def test_queued_jobs_run_before_a_pending_check():
+    # job 0 has a long check; job 1 is queued when job 0's energies are ready: it runs first
+    arr = np.array([0.0, 0.05, 5.0])
+    nb = np.array([10, 10, 10], dtype=np.int64)
+    svc = np.array([0.1, 0.1, 0.1])
+    chk = np.array([10.0, -1.0, -1.0])
+    start, ready, done = _check_deferred(arr, nb, svc, chk, 1000, 1)
+    assert start[1] == pytest.approx(0.1) and done[0] == pytest.approx(0.2 + 10.0)
+    # one slot and a running check: a later job waits for it (checks are not preempted)
+    assert start[2] == pytest.approx(10.2)
+    # two slots: the later job starts on arrival beside the check
+    start2, _, _ = _check_deferred(arr, nb, svc, chk, 1000, 2)
+    assert start2[2] == pytest.approx(5.0)
+
+
+def test_held_bytes_never_deadlock_the_queue():
+    # every job is checked and the budget holds two: checks run whenever the head cannot fit
+    n = 12
+    arr = np.zeros(n)
+    nb = np.full(n, 40, dtype=np.int64)
+    svc = np.full(n, 0.1)
+    chk = np.full(n, 0.5)
+    start, ready, done = _check_deferred(arr, nb, svc, chk, 100, 4)
+    assert np.all(done > 0) and done.max() < 1e3
