@@ -41,7 +41,9 @@ SEED = 1
 WORKLOAD = ("o40v300 tiled FP64 drop-in: o=40 as 8/12/20, v=300 as 20,24x5,30x4,40, seed 1; "
             "step = one of 128 strided slices of the 2860-tuple weight-ordered list")
 METRIC = "(T) TFLOP/s"
-# ncu, fused_fp64_kernel on 2 tuples of o40v114 (profiles/fused_fp64_kernel_o40v114_2tuples.md)
+# DRAM bytes per algorithmic FLOP of fused_fp64_kernel: ncu dram__bytes_read.sum +
+# dram__bytes_write.sum (327.9 MB + 26.2 MB) over one launch on 2 tuples of the
+# o=40/v=114 case (2.587e11 FLOPs)
 FP64_DRAM_BYTES_PER_FLOP = (327.9e6 + 26.2e6) / 2.587e11
 MIXED_FORMS = (("tf32", 1), ("bf16", 2), ("fp16", 3))
 MIXED_NOTE = {"tf32": "TF32x3: TF32 hi/lo pairs, kind::tf32", "bf16": "BF16x3: bf16 hi/lo pairs, kind::f16",
@@ -377,7 +379,7 @@ def profile_case(args) -> None:  # noqa: C901
     with ng.TriplesJob(t) as job:
         job.load(*files)
         job.set_timing(True)
-        job.set_mixed_cluster(args.shape)
+        job.set_mixed_shape(args.shape)
         prec = dict(MIXED_FORMS).get(args.mixed, ng.PREC_FP64)
         job.run(sel, precision=prec)
         e = job.run(sel, precision=prec)
@@ -616,7 +618,7 @@ def main() -> None:
     ap.add_argument("--check-every", type=int, default=100, help="serve: FP64 check on every n-th job (0: none)")
     ap.add_argument("--max-ctas", type=int, default=0, help="serve: CTA cap per job launch (0: all SMs)")
     ap.add_argument("--case", default="o40v114", choices=["o40v114", "o64v128", "sym8s"], help="--profile case")
-    ap.add_argument("--shape", type=int, default=1, choices=[1, 2, 4], help="mixed work-unit shape")
+    ap.add_argument("--shape", type=int, default=1, choices=[1, 2], help="mixed work-unit shape")
     ap.add_argument("--kseg", type=int, default=0, help="mixed form: K chunks per accumulator drain")
     ap.add_argument("--mixed", default="", choices=["", "tf32", "bf16", "fp16"],
                     help="--profile case in a mixed form")

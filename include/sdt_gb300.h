@@ -232,10 +232,8 @@ int sdt_job_set_mixed_segment(sdt_job *job, int chunks);
  * sub-box, the finished sub-box kept in registers while the next one is
  * contracted; 2: the same with the finished sub-box kept in tensor memory
  * (one accumulator instead of two, the energy work gets the registers --
- * for tuples whose spin/irrep-kept K is short); 4: clusters of 4 CTAs whose
- * sub-boxes differ in the j and k boxes and that multicast the operand
- * tiles they share. */
-int sdt_job_set_mixed_cluster(sdt_job *job, int ctas);
+ * for tuples whose spin/irrep-kept K is short). */
+int sdt_job_set_mixed_shape(sdt_job *job, int shape);
 /* When on, sdt_job_run brackets its fused-kernel launches with CUDA events
  * on the run's stream; sdt_job_last_kernel_ms returns that interval. */
 int sdt_job_set_timing(sdt_job *job, int on);
@@ -244,8 +242,8 @@ double sdt_job_last_kernel_ms(const sdt_job *job);
 /* Plans (no reference counterpart): a prepared evaluation of a tuple
  * list.  sdt_plan_create checks the list, builds the work indexes, sizes
  * the persistent launches (and, for a mixed precision, encodes the job's
- * split operands if needed) and uploads them; ctas (optional, one per
- * tuple: 1, 2 or 4 as in sdt_job_set_mixed_cluster) picks the mixed
+ * split operands if needed) and uploads them; shapes (optional, one per
+ * tuple: 1 or 2 as in sdt_job_set_mixed_shape) picks the mixed
  * kernel's work-unit shape per tuple.
  * sdt_plan_launch only enqueues device work -- per group a queue reset and
  * one persistent kernel, the compensated sums and the copy of the results
@@ -256,7 +254,7 @@ double sdt_job_last_kernel_ms(const sdt_job *job);
  * order.  A plan is bound to its job; destroy it after its last run. */
 typedef struct sdt_plan sdt_plan;
 int sdt_plan_create(sdt_job *job, const int64_t *klist, int64_t n,
-                    int precision, const int32_t *ctas, sdt_plan **plan);
+                    int precision, const int32_t *shapes, sdt_plan **plan);
 int sdt_plan_launch(sdt_plan *plan, void *stream);
 int sdt_plan_capture(sdt_plan *plan, void *stream);
 int sdt_plan_run(sdt_plan *plan, void *stream, double *energy,

@@ -57,7 +57,7 @@ def _declare(lib):
         "sdt_launch_count": (I64, []),
         "sdt_job_set_timing": (C.c_int, [C.c_void_p, C.c_int]),
         "sdt_job_set_mixed_segment": (C.c_int, [C.c_void_p, C.c_int]),
-        "sdt_job_set_mixed_cluster": (C.c_int, [C.c_void_p, C.c_int]),
+        "sdt_job_set_mixed_shape": (C.c_int, [C.c_void_p, C.c_int]),
         "sdt_job_last_kernel_ms": (C.c_double, [C.c_void_p]),
         "sdt_probe_fp64_tflops": (C.c_double, [C.c_int]),
         "sdt_plan_create": (C.c_int, [C.c_void_p, PI64, C.c_int64, C.c_int, C.POINTER(C.c_int32),

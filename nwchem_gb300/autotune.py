@@ -5,17 +5,15 @@ the batched path also chooses, per job, which split encoding runs the d1/d2
 contractions (TF32x3, BF16x3 or scaled FP16x3, among the forms the caller's
 accuracy allows) and, per size class of tuples, the kernel's work-unit
 shape: one 8x8x8x4x4x4 sub-box per CTA with the finished sub-box held in
-registers (two tensor-memory accumulators), the same with it held in tensor
-memory (one accumulator, free registers for the FP64 energy work), or a 2x2
-tile of (j,k) sub-boxes per cluster of 4 CTAs that multicast the operand
-tiles they share.
+registers (two tensor-memory accumulators), or the same with it held in
+tensor memory (one accumulator, free registers for the FP64 energy work).
 
 A size class is the pair (log2 of the tuple's virtual sub-box count,
 log2 of its occupied sub-box count), rounded.  For each class the tuner
 times every candidate on up to `sample` tuples of the class (evenly spaced
 in the list) and keeps the one with the least time per algorithmic FLOP.
 Decisions can be cached in a JSON file keyed by the tiling.  The timing
-function is injectable (measure(klist, precision, ctas) -> seconds), which
+function is injectable (measure(klist, precision, shape) -> seconds), which
 is how the host logic is tested without a GPU.
 """
 from __future__ import annotations
@@ -32,7 +30,7 @@ from .tiling import Tiling
 from .triples import PREC_MIXED_BF16, PREC_MIXED_FP16, PREC_MIXED_TF32, Plan, TriplesJob, flops
 
 FORMS = {"tf32": PREC_MIXED_TF32, "bf16": PREC_MIXED_BF16, "fp16": PREC_MIXED_FP16}
-SHAPES = (1, 2, 4)  # work-unit shapes: 1 CTA, 1 CTA with the sub-box kept in TMEM, cluster of 4
+SHAPES = (1, 2)  # work-unit shapes: the finished sub-box kept in registers, or in TMEM
 
 Measure = Callable[[np.ndarray, int, int], float]
 
@@ -70,17 +68,17 @@ class Autotuner:
         self.log: list[dict] = []
 
     # -- measurement ---------------------------------------------------------
-    def _measure_gpu(self, klist: np.ndarray, precision: int, ctas: int) -> float:
+    def _measure_gpu(self, klist: np.ndarray, precision: int, shape: int) -> float:
         self.job.set_timing(True)
-        with Plan(self.job, klist, precision, np.full(len(klist), ctas, dtype=np.int32)) as p:
+        with Plan(self.job, klist, precision, np.full(len(klist), shape, dtype=np.int32)) as p:
             p.run()
             p.run()
         return self.job.last_kernel_ms / 1e3
 
-    def _cost(self, klist: np.ndarray, precision: int, ctas: int) -> float:
-        sec = self.measure(klist, precision, ctas)
+    def _cost(self, klist: np.ndarray, precision: int, shape: int) -> float:
+        sec = self.measure(klist, precision, shape)
         per = sec / max(flops(self.tiling, klist), 1.0)
-        self.log.append({"tuples": int(len(klist)), "precision": precision, "ctas": ctas, "s_per_flop": per})
+        self.log.append({"tuples": int(len(klist)), "precision": precision, "shape": shape, "s_per_flop": per})
         return per
 
     # -- classes ---------------------------------------------------------------
@@ -116,7 +114,7 @@ class Autotuner:
 
     # -- decisions -------------------------------------------------------------
     def tune(self, klist: np.ndarray) -> dict:
-        """{'form': name, 'shapes': {class: ctas}} for this tuple list."""
+        """{'form': name, 'shapes': {class: shape}} for this tuple list."""
         klist = np.ascontiguousarray(klist, dtype=np.int64).reshape(-1, 7)
         cached = self._load()
         classes = self.classes(klist)
@@ -135,14 +133,14 @@ class Autotuner:
         self._store(entry)
         return entry
 
-    def ctas(self, klist: np.ndarray, decision: dict) -> np.ndarray:
+    def shapes(self, klist: np.ndarray, decision: dict) -> np.ndarray:
         return np.array([decision["shapes"][size_class(self.tiling, k)] for k in klist], dtype=np.int32)
 
     def plan(self, klist: np.ndarray, capture: bool = True, stream=None) -> tuple[Plan, dict]:
         """A plan of the whole list with the tuned choices (CUDA graph captured)."""
         klist = np.ascontiguousarray(klist, dtype=np.int64).reshape(-1, 7)
         d = self.tune(klist)
-        p = Plan(self.job, klist, FORMS[d["form"]], self.ctas(klist, d))
+        p = Plan(self.job, klist, FORMS[d["form"]], self.shapes(klist, d))
         if capture:
             p.capture(stream)
         return p, d

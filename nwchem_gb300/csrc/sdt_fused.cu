@@ -845,10 +845,10 @@ extern "C" int sdt_job_set_max_ctas(sdt_job *j, int sms) {
 
 extern "C" void *sdt_job_stream(const sdt_job *j) { return j ? (void *)j->stream : nullptr; }
 
-extern "C" int sdt_job_set_mixed_cluster(sdt_job *j, int ctas) {
-    if (!j || (ctas != 1 && ctas != 2 && ctas != 4))
-        return fail(SDT_ERR_ARG, "sdt_job_set_mixed_cluster: shape 1, 2 or 4");
-    j->mixed_cluster = ctas;
+extern "C" int sdt_job_set_mixed_shape(sdt_job *j, int shape) {
+    if (!j || (shape != 1 && shape != 2))
+        return fail(SDT_ERR_ARG, "sdt_job_set_mixed_shape: shape 1 or 2");
+    j->mixed_shape = shape;
     return SDT_OK;
 }
 

@@ -41,7 +41,7 @@ struct sdt_job {
     int64_t tile_box_off = 0, pair_blk_off = 0;
     int32_t nob = 0, nvb = 0;            // hole and particle boxes over all tiles
     int mixed_kseg = 0;                  // K chunks per TMEM drain (0: whole term)
-    int mixed_cluster = 1;               // CTAs per cluster of the mixed kernel: 1 or 4
+    int mixed_shape = 1;                 // work-unit shape of the mixed kernel: 1 register hold, 2 tensor-memory hold
     int all_k = 1;                       // every K tile allowed for every term
     bool loaded = false;
     // optional CUDA-event timing of the fused launches of the last run
@@ -55,18 +55,17 @@ namespace sdt {
 // Multiplicity factor of a tuple (ccsd_t_dot.F:52-66).
 double tuple_factor(const int64_t *k, bool restricted);
 
-// One persistent launch over a contiguous group of tuples.  Prefix arrays
-// are relative to the group: item_pref[q] (and, mixed form, super_pref[q],
-// the cluster work units) count from zero; part receives the group's item
-// pairs.
+// One persistent launch over a contiguous group of tuples.  The item prefix
+// is relative to the group (item_pref[0] = 0); part receives the group's
+// item pairs.
 struct LaunchArgs {
-    const int64_t *klist = nullptr, *item_pref = nullptr, *super_pref = nullptr;
+    const int64_t *klist = nullptr, *item_pref = nullptr;
     const double *factor = nullptr;
     double *part = nullptr;
-    int64_t n = 0, items = 0, n_super = 0;
+    int64_t n = 0, items = 0;
     unsigned long long *queue = nullptr;  // work counter, reset by the launch
     int *err = nullptr;                   // mixed form: wait-timeout code, reset by the launch
-    int cluster = 1, grid = 1;
+    int shape = 1, grid = 1;              // mixed form: work-unit shape 1 or 2
 };
 
 // Per-tuple compensated sums of item pairs (gpref: global item prefix, n+1)
@@ -79,8 +78,8 @@ void mixed_release(sdt_job *j);
 // Builds the split operands of element type `type` (TM_*) and the box
 // tables (after a successful load).
 int mixed_prepare(sdt_job *j, int type, cudaStream_t st);
-// Grid of the mixed kernel for a group (sets the kernel's shared-memory
-// attribute; call outside stream capture).
-int mixed_grid(sdt_job *j, int cluster, int64_t n_super, int *grid);
+// Grid of the mixed kernel for a group of work-unit shape 1 or 2 (sets the
+// kernel's shared-memory attribute; call outside stream capture).
+int mixed_grid(sdt_job *j, int shape, int64_t n_items, int *grid);
 int mixed_launch(sdt_job *j, const LaunchArgs &a, cudaStream_t st);
 }  // namespace sdt

@@ -1,9 +1,9 @@
 // sdt_plan.cu -- prepared evaluations of tuple lists (plans) and the job run.
 //
 // A plan does the host work of a run once: it checks the tuple list, builds
-// the item and work-unit prefixes and the multiplicity factors, groups the
-// tuples by work-unit shape (single sub-boxes, or 2x2 (j,k) sub-box tiles
-// taken by clusters of 4 CTAs), uploads everything and sizes every launch.
+// the item prefixes and the multiplicity factors, groups the tuples by the
+// mixed kernel's work-unit shape (the finished sub-box kept in registers or
+// in tensor memory), uploads everything and sizes every launch.
 // sdt_plan_launch then only enqueues device work -- per group a queue reset
 // and one persistent launch, the per-tuple and total compensated sums, and
 // the copy of the results to pinned host memory -- so a launch can be
@@ -23,12 +23,12 @@ struct sdt_plan {
     int64_t n = 0, items = 0;
     std::vector<int64_t> order;  // plan position -> caller's tuple index
     struct Group {
-        int cluster = 1, grid = 1;
-        int64_t t0 = 0, t1 = 0, i0 = 0, items = 0, n_super = 0;
+        int shape = 1, grid = 1;
+        int64_t t0 = 0, t1 = 0, i0 = 0, items = 0;
     };
     std::vector<Group> groups;
     // device
-    int64_t *klist_d = nullptr, *rpref_d = nullptr, *spref_d = nullptr, *gpref_d = nullptr;
+    int64_t *klist_d = nullptr, *rpref_d = nullptr, *gpref_d = nullptr;
     double *factor_d = nullptr, *part_d = nullptr, *task_d = nullptr, *out_d = nullptr;
     unsigned long long *queue_d = nullptr;  // one counter per group
     int *err_d = nullptr;
@@ -49,7 +49,6 @@ void plan_free(sdt_plan *p) {
     if (p->graph) cudaGraphDestroy(p->graph);
     gpu_put(p->klist_d);
     gpu_put(p->rpref_d);
-    gpu_put(p->spref_d);
     gpu_put(p->gpref_d);
     gpu_put(p->factor_d);
     gpu_put(p->part_d);
@@ -66,10 +65,10 @@ int mixed_type_of(int precision) {
     return precision == SDT_PREC_MIXED_TF32 ? TM_F32 : precision == SDT_PREC_MIXED_BF16 ? TM_BF16 : TM_F16;
 }
 
-// Builds a plan; ctas[q] (optional, caller order) is the work-unit shape of
-// tuple q: 1 one CTA per sub-box, 2 the same with the finished sub-box kept in
-// tensor memory, 4 clusters of 4 CTAs on 2x2 (j,k) sub-box tiles.
-int plan_create(sdt_job *j, const int64_t *klist, int64_t n, int precision, const int32_t *ctas,
+// Builds a plan; shapes[q] (optional, caller order) is the work-unit shape of
+// tuple q in the mixed form: 1 the finished sub-box in the energy warps'
+// registers, 2 the finished sub-box kept in tensor memory.
+int plan_create(sdt_job *j, const int64_t *klist, int64_t n, int precision, const int32_t *shapes,
                 sdt_plan **out, const char *who) {
     *out = nullptr;
     if (!j || (n > 0 && !klist)) return fail(SDT_ERR_ARG, std::string(who) + ": null argument");
@@ -88,54 +87,49 @@ int plan_create(sdt_job *j, const int64_t *klist, int64_t n, int precision, cons
         }
         if (!(k[0] <= k[1] && k[1] <= k[2] && k[3] <= k[4] && k[4] <= k[5]))
             return fail(SDT_ERR_ARG, std::string(who) + ": tuple tiles not sorted");
-        if (ctas && ctas[q] != 1 && ctas[q] != 2 && ctas[q] != 4)
-            return fail(SDT_ERR_ARG, std::string(who) + ": work-unit shape must be 1, 2 or 4");
+        if (shapes && shapes[q] != 1 && shapes[q] != 2)
+            return fail(SDT_ERR_ARG, std::string(who) + ": work-unit shape must be 1 or 2");
     }
     sdt_plan *p = new sdt_plan();
     p->job = j;
     p->precision = precision;
     p->n = n;
-    // Group by cluster size (FP64: one group), keeping the caller's order inside a group.
-    auto cl = [&](int64_t q) { return mixed ? (ctas ? (int)ctas[q] : j->mixed_cluster) : 1; };
-    for (int c : {1, 2, 4})
+    // Group by work-unit shape (FP64: one group), keeping the caller's order inside a group.
+    auto cl = [&](int64_t q) { return mixed ? (shapes ? (int)shapes[q] : j->mixed_shape) : 1; };
+    for (int c : {1, 2})
         for (int64_t q = 0; q < n; ++q)
             if (cl(q) == c) p->order.push_back(q);
     const int box_v = mixed ? 8 : 4, box_o = 4;
-    std::vector<int64_t> kl(7 * std::max<int64_t>(n, 1)), rpref, spref, gpref(n + 1, 0);
+    std::vector<int64_t> kl(7 * std::max<int64_t>(n, 1)), rpref, gpref(n + 1, 0);
     std::vector<double> fac(std::max<int64_t>(n, 1));
     for (int64_t pos = 0; pos < n;) {
         sdt_plan::Group g;
-        g.cluster = cl(p->order[pos]);
+        g.shape = cl(p->order[pos]);
         g.t0 = pos;
         g.i0 = gpref[pos];
         rpref.push_back(0);
-        spref.push_back(0);
-        while (pos < n && cl(p->order[pos]) == g.cluster) {
+        while (pos < n && cl(p->order[pos]) == g.shape) {
             const int64_t *k = klist + 7 * p->order[pos];
             std::memcpy(kl.data() + 7 * pos, k, 7 * sizeof(int64_t));
-            int64_t boxes = 1, supers = 1;
+            int64_t boxes = 1;
             for (int d = 0; d < 6; ++d) {
                 const int bx = d < 3 ? box_v : box_o;
                 const int64_t nb = (t.r(k[d]) + bx - 1) / bx;
                 boxes *= nb;
-                supers *= (d >= 4 && g.cluster == 4) ? (nb + 1) / 2 : nb;
             }
             fac[pos] = tuple_factor(k, t.restricted != 0);
             gpref[pos + 1] = gpref[pos] + boxes;
             rpref.push_back(rpref.back() + boxes);
-            spref.push_back(spref.back() + supers);
             ++pos;
         }
         g.t1 = pos;
         g.items = rpref.back();
-        g.n_super = spref.back();
         p->groups.push_back(g);
     }
     p->items = gpref[n];
     const size_t ng = std::max<size_t>(p->groups.size(), 1);
     p->klist_d = (int64_t *)gpu_get(kl.size() * sizeof(int64_t));
     p->rpref_d = (int64_t *)gpu_get(std::max<size_t>(rpref.size(), 1) * sizeof(int64_t));
-    p->spref_d = (int64_t *)gpu_get(std::max<size_t>(spref.size(), 1) * sizeof(int64_t));
     p->gpref_d = (int64_t *)gpu_get(gpref.size() * sizeof(int64_t));
     p->factor_d = (double *)gpu_get(fac.size() * sizeof(double));
     p->part_d = (double *)gpu_get(std::max<int64_t>(2 * p->items, 2) * sizeof(double));
@@ -145,7 +139,7 @@ int plan_create(sdt_job *j, const int64_t *klist, int64_t n, int precision, cons
     p->err_d = (int *)gpu_get(sizeof(int));
     p->host_out = (double *)host_get((2 + 2 * std::max<int64_t>(n, 1)) * sizeof(double));
     p->err_h = (int *)host_get(sizeof(int));
-    if (!p->klist_d || !p->rpref_d || !p->spref_d || !p->gpref_d || !p->factor_d || !p->part_d || !p->task_d ||
+    if (!p->klist_d || !p->rpref_d || !p->gpref_d || !p->factor_d || !p->part_d || !p->task_d ||
         !p->out_d || !p->queue_d || !p->err_d || !p->host_out || !p->err_h) {
         plan_free(p);
         return fail(SDT_ERR_NOMEM, std::string(who) + ": plan buffers");
@@ -167,12 +161,11 @@ int plan_create(sdt_job *j, const int64_t *klist, int64_t n, int precision, cons
     };
     up(p->klist_d, kl.data(), 7 * n * sizeof(int64_t));
     up(p->rpref_d, rpref.data(), rpref.size() * sizeof(int64_t));
-    up(p->spref_d, spref.data(), spref.size() * sizeof(int64_t));
     up(p->gpref_d, gpref.data(), gpref.size() * sizeof(int64_t));
     up(p->factor_d, fac.data(), n * sizeof(double));
     for (auto &g : p->groups) {
         if (rc) break;
-        rc = mixed ? mixed_grid(j, g.cluster, g.n_super, &g.grid) : fp64_grid(j, g.items, &g.grid);
+        rc = mixed ? mixed_grid(j, g.shape, g.items, &g.grid) : fp64_grid(j, g.items, &g.grid);
         p->kernels += 1;
     }
     p->kernels += (n + 65534) / 65535 + 1;  // tuple sums and the total
@@ -208,15 +201,13 @@ int plan_enqueue(sdt_plan *p, cudaStream_t st) {
         LaunchArgs a;
         a.klist = p->klist_d + 7 * g.t0;
         a.item_pref = p->rpref_d + g.t0 + gi;
-        a.super_pref = p->spref_d + g.t0 + gi;
         a.factor = p->factor_d + g.t0;
         a.part = p->part_d + 2 * g.i0;
         a.n = g.t1 - g.t0;
         a.items = g.items;
-        a.n_super = g.n_super;
         a.queue = p->queue_d + gi;
         a.err = p->err_d;
-        a.cluster = g.cluster;
+        a.shape = g.shape;
         a.grid = g.grid;
         rc = p->mtype >= 0 ? mixed_launch(j, a, st) : fp64_launch(j, a, st);
     }
@@ -257,10 +248,10 @@ int plan_read(sdt_plan *p, cudaStream_t st, double *energy, double *per_task, co
 
 using namespace sdt;
 
-extern "C" int sdt_plan_create(sdt_job *job, const int64_t *klist, int64_t n, int precision, const int32_t *ctas,
+extern "C" int sdt_plan_create(sdt_job *job, const int64_t *klist, int64_t n, int precision, const int32_t *shapes,
                                sdt_plan **plan) {
     if (!plan) return fail(SDT_ERR_ARG, "sdt_plan_create: null output");
-    return plan_create(job, klist, n, precision, ctas, plan, "sdt_plan_create");
+    return plan_create(job, klist, n, precision, shapes, plan, "sdt_plan_create");
 }
 
 extern "C" int sdt_plan_launch(sdt_plan *plan, void *stream) {

@@ -174,7 +174,7 @@ void run_one(sdt_server *s, sdt_server::Job *job) {
         failed(rc);
         return;
     }
-    if (job->precision != SDT_PREC_FP64) sdt_job_set_mixed_cluster(j, mixed_shape(&job->t));
+    if (job->precision != SDT_PREC_FP64) sdt_job_set_mixed_shape(j, mixed_shape(&job->t));
     rc = sdt_job_load(j, &job->f1, &job->f2, &job->fv, nullptr);
     job->t_loaded = s->now();
     int64_t n = 0;

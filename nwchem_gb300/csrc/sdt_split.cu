@@ -4,21 +4,9 @@
 // the latter overlapped with the next sub-box's contractions.
 //
 // Work unit (item): an 8x8x8 (a,b,c) x 4x4x4 (i,j,k) sub-box of one tuple's
-// triples tile, 32768 values.  The kernel runs in clusters of 4 CTAs (one CTA
-// per SM) that take the 4 items of a "super-item" -- the same (a,b,c,i)
-// boxes, j boxes 2J+rj and k boxes 2K+rk (rj, rk in {0,1}, cluster rank
-// 2*rj+rk).  Super-items are dealt to the clusters round-robin
-// (super = cluster id + n * clusters), so results do not depend on timing.
-//
-// Operand sharing.  A merged term's A operand depends on its two row holes
-// and its B operand on its column hole.  Inside a cluster, an operand that
-// does not involve j or k is the same for all 4 CTAs, one that involves only
-// k (or only j) is the same for the 2 CTAs with the same rk (rj): each CTA
-// loads its quarter or half of every shared tile and multicasts it to the
-// CTAs that share it (TMA .multicast::cluster), so every CTA receives full
-// tiles while the L2 serves half the bytes.  A stage is refilled only after
-// all 4 CTAs' MMAs have released it (their tcgen05.commit arrives on the
-// stage's empty barrier in every CTA of the cluster).
+// triples tile, 32768 values.  One CTA per SM; CTAs draw items from a device
+// queue (one atomic counter) until it is empty.  Each item's result depends
+// only on its index, so results do not depend on timing.
 //
 // Contractions.  Every d1 term has exactly the row/column index layout and the
 // sign of one d2 term (d1_1/d2_8, d1_2/d2_9, d1_3/d2_7, d1_4/d2_2, d1_5/d2_3,
@@ -162,33 +150,33 @@ struct SplitParams {
     const int32_t *tiles;         // [ntiles][4] start, range, spin, sym
     int32_t noab, nvab, nk_o, nk_v, kseg, nob, nvb;
     int64_t nocc, nvir;
-    const int64_t *klist, *item_pref, *super_pref;
+    const int64_t *klist, *item_pref;
     const double *factor;
-    int64_t n_tasks, n_super;
+    int64_t n_tasks, n_items;
     double inv_s, inv_s2;         // undo the operand scaling (FP16): X_true = X * inv_s
     double *part;
     int *err;
-    unsigned long long *queue;    // work-unit counter (single CTAs), zero at launch
+    unsigned long long *queue;    // item counter, zero at launch
     int32_t all_k;                // every K tile allowed for every term (one spin, no irreps)
 };
 
 struct ItemBox {
     int tile[6], start[6], ext[6], boff[6], lbox[6];  // lbox: local box, clamped into the tile
-    int64_t tq, item;  // item = -1: this CTA's box lies outside the tuple
+    int64_t tq, item;
 };
 
-// Decodes work unit si.  PJ = 2 (clusters of 4): the unit is a super-item and
-// this CTA takes j box 2J+rj and k box 2K+rk; PJ = 1: the unit is one item.
-template <int PJ>
-__device__ __forceinline__ void decode_super(const SplitParams &p, int64_t si, int rj, int rk, ItemBox &b) {
+// Decodes item si: its tuple (binary search of the item prefix) and its
+// sub-box, k box fastest.
+__device__ __forceinline__ void decode_item(const SplitParams &p, int64_t si, ItemBox &b) {
     int64_t lo = 0, hi = p.n_tasks - 1;
     while (lo < hi) {
         const int64_t mid = (lo + hi + 1) >> 1;
-        if (p.super_pref[mid] <= si) lo = mid;
+        if (p.item_pref[mid] <= si) lo = mid;
         else hi = mid - 1;
     }
     b.tq = lo;
-    int64_t local = si - p.super_pref[lo];
+    b.item = si;
+    int64_t local = si - p.item_pref[lo];
     int nb[6];
 #pragma unroll
     for (int d = 0; d < 6; ++d) {
@@ -199,28 +187,15 @@ __device__ __forceinline__ void decode_super(const SplitParams &p, int64_t si, i
         nb[d] = (b.ext[d] + bx - 1) / bx;
     }
     int box[6];
-    const int nk2 = (nb[5] + PJ - 1) / PJ, nj2 = (nb[4] + PJ - 1) / PJ;
-    box[5] = PJ * (int)(local % nk2) + rk;
-    local /= nk2;
-    box[4] = PJ * (int)(local % nj2) + rj;
-    local /= nj2;
 #pragma unroll
-    for (int d = 3; d >= 0; --d) {
+    for (int d = 5; d >= 0; --d) {
         box[d] = (int)(local % nb[d]);
         local /= nb[d];
     }
 #pragma unroll
     for (int d = 0; d < 6; ++d) {
         b.boff[d] = box[d] * (d < 3 ? SX_BV : SX_BO);
-        b.lbox[d] = min(box[d], nb[d] - 1);
-    }
-    if (box[4] < nb[4] && box[5] < nb[5]) {
-        int64_t x = box[0];
-#pragma unroll
-        for (int d = 1; d < 6; ++d) x = x * nb[d] + box[d];
-        b.item = p.item_pref[lo] + x;
-    } else {
-        b.item = -1;
+        b.lbox[d] = box[d];
     }
 }
 
@@ -274,10 +249,9 @@ __device__ __forceinline__ int term_segments(int nk, int kseg_req, int &kseg) {
     return nk > 0 ? (nk + kseg - 1) / kseg : 1;
 }
 
-// Work units of a CTA.  Clusters (CS = 4) walk a fixed round-robin list;
-// single CTAs draw from the device queue: the producer thread takes the next
-// unit and publishes it in a 4-slot ring (id, or -1 at the end), which the MMA
-// thread, the drain leader and the energy leader each read and release.
+// Items of a CTA: the producer thread takes the next item from the device
+// queue and publishes it in a 4-slot ring (id, or -1 at the end), which the
+// MMA thread, the drain leader and the energy leader each read and release.
 constexpr int SX_RING = 4;
 struct UnitRing {
     int64_t *id;
@@ -314,58 +288,32 @@ __device__ __forceinline__ void bulk_load(void *dst, const void *src, uint32_t b
                  ::"r"(tc::smem_u32(dst)), "l"(src), "r"(bytes), "r"(tc::smem_u32(bar))
                  : "memory");
 }
-__device__ __forceinline__ void bulk_load_mc(void *dst, const void *src, uint32_t bytes, uint64_t *bar,
-                                             uint16_t mask) {
-    asm volatile(
-        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes.multicast::cluster [%0], [%1], %2, [%3], %4;"
-        ::"r"(tc::smem_u32(dst)), "l"(src), "r"(bytes), "r"(tc::smem_u32(bar)), "h"(mask)
-        : "memory");
-}
 
 // ---------------------------------------------------------------------------
 // Operand producer (one thread): per stage, the A and B blocks (hi, lo) of
-// the term's K chunk.  With clusters of 4 (CS = 4), per merged term and rank
-// (rj, rk):
-//   rows (x;j,k) [terms 0,3,6]: A own;  B shared by all 4: quarter `rank`;
-//   rows (x;i,k) [terms 1,4,7]: A shared by the two CTAs with this rk: half rj;
-//       B (column hole j) shared by the two with this rj: half rk;
-//   rows (x;i,j) [terms 2,5,8]: A shared by the two with this rj: half rk;
-//       B (column hole k) shared by the two with this rk: half rj;
-// each piece is multicast to the CTAs that share it.  Halves and quarters
-// split the slowest row index (R0 of A, C0 of B): contiguous runs of a block.
-template <int TYPE, int CS>
+// the term's K chunk, four contiguous bulk copies.
+template <int TYPE>
 __device__ __forceinline__ void run_producer(const SplitParams &p, uint8_t *stages, uint64_t *full,
-                                             uint64_t *empty, volatile int *abort, int rj, int rk,
-                                             int64_t unit0, int64_t ustep, const UnitRing &ring) {
-    constexpr int PJ = CS == 4 ? 2 : 1;
+                                             uint64_t *empty, volatile int *abort, const UnitRing &ring) {
     constexpr int KE = TYPE == TM_F32 ? 8 : 16;  // K values per 32-byte row
-    const int rank = 2 * rj + rk;
-    const uint16_t m_all = 0xF, m_rk = (uint16_t)((1u << rk) | (1u << (2 + rk))), m_rj = (uint16_t)(3u << (2 * rj));
     const int64_t NOB = p.nob, NVB = p.nvb;
     uint32_t g = 0;
     bool stop = false;
     for (int n = 0; !stop; ++n) {
-        int64_t si;
-        if (CS == 1) {
-            const unsigned long long u = atomicAdd(p.queue, 1ull);
-            si = u < (unsigned long long)p.n_super ? (int64_t)u : -1;
-            if (!ring_publish(ring, n, si, abort)) {
-                stop = true;
-                break;
-            }
-            if (si < 0) break;
-        } else {
-            si = unit0 + (int64_t)n * ustep;
-            if (si >= p.n_super) break;
+        const unsigned long long u = atomicAdd(p.queue, 1ull);
+        const int64_t si = u < (unsigned long long)p.n_items ? (int64_t)u : -1;
+        if (!ring_publish(ring, n, si, abort)) {
+            stop = true;
+            break;
         }
+        if (si < 0) break;
         ItemBox bx;
-        decode_super<PJ>(p, si, rj, rk, bx);
+        decode_item(p, si, bx);
         int gb[6];  // global box ids
 #pragma unroll
         for (int d = 0; d < 6; ++d) gb[d] = __ldg(p.tile_box + bx.tile[d] - 1) + bx.lbox[d];
         for (int t = 0; t < 9 && !stop; ++t) {
             const MergedTerm td = kMerged[t];
-            const int ty = t % 3;
             // first blocks (K chunk 0) of the term's d1 and d2 operands
             const int64_t arow = ((int64_t)gb[td.r[0]] * NOB + gb[td.r[1]]) * NOB + gb[td.r[2]];
             const int64_t a1 = arow * p.nk_o, a2 = arow * p.nk_v;
@@ -374,12 +322,6 @@ __device__ __forceinline__ void run_producer(const SplitParams &p, uint8_t *stag
             const int nbc1 = (__ldg(p.tiles + 4 * (tc1 - 1) + 1) + SX_BV - 1) / SX_BV;
             const int64_t b2 = __ldg(p.pair_blk + (bx.tile[td.c[0]] - p.noab - 1) * p.nvab + (tc1 - p.noab - 1)) +
                                (((int64_t)bx.lbox[td.c[0]] * nbc1 + bx.lbox[td.c[1]]) * NOB + gb[td.c[2]]) * p.nk_v;
-            // this CTA's piece of A (ha < 0: whole) and of B (piece hb of nbp)
-            const int ha = (CS == 1 || ty == 0) ? -1 : ty == 1 ? rj : rk;
-            const uint16_t ma = ty == 1 ? m_rk : m_rj;
-            const int nbp = CS == 1 ? 1 : ty == 0 ? 4 : 2;
-            const int hb = CS == 1 ? 0 : ty == 0 ? rank : ty == 1 ? rk : rj;
-            const uint16_t mb = ty == 0 ? m_all : ty == 1 ? m_rj : m_rk;
             for (int part = 0; part < 2 && !stop; ++part) {
                 const int la = part == 0 ? L_WD1 : L_T2B, lb = part == 0 ? L_T2A : L_VD2;
                 const int64_t abase = part == 0 ? a1 : a2, bbase = part == 0 ? b1 : b2;
@@ -392,26 +334,12 @@ __device__ __forceinline__ void run_producer(const SplitParams &p, uint8_t *stag
                     }
                     ++g;
                     uint8_t *st = stages + s * SX_STAGE;
-                    tc::mbar_arrive_expect_tx(&full[s], SX_STAGE);  // this CTA's whole stage, from all issuers
+                    tc::mbar_arrive_expect_tx(&full[s], SX_STAGE);
                     const int64_t ab = abase + c, bb = bbase + c;
-                    const uint8_t *ah = p.blk[2 * la] + ab * SX_A, *al = p.blk[2 * la + 1] + ab * SX_A;
-                    const uint8_t *bh = p.blk[2 * lb] + bb * SX_B, *bl = p.blk[2 * lb + 1] + bb * SX_B;
-                    if (ha < 0) {
-                        bulk_load(st, ah, SX_A, &full[s]);
-                        bulk_load(st + SX_A, al, SX_A, &full[s]);
-                    } else {
-                        const int off = ha * (SX_A / 2);
-                        bulk_load_mc(st + off, ah + off, SX_A / 2, &full[s], ma);
-                        bulk_load_mc(st + SX_A + off, al + off, SX_A / 2, &full[s], ma);
-                    }
-                    if (nbp == 1) {
-                        bulk_load(st + 2 * SX_A, bh, SX_B, &full[s]);
-                        bulk_load(st + 2 * SX_A + SX_B, bl, SX_B, &full[s]);
-                    } else {
-                        const int piece = SX_B / nbp, off = hb * piece;
-                        bulk_load_mc(st + 2 * SX_A + off, bh + off, piece, &full[s], mb);
-                        bulk_load_mc(st + 2 * SX_A + SX_B + off, bl + off, piece, &full[s], mb);
-                    }
+                    bulk_load(st, p.blk[2 * la] + ab * SX_A, SX_A, &full[s]);
+                    bulk_load(st + SX_A, p.blk[2 * la + 1] + ab * SX_A, SX_A, &full[s]);
+                    bulk_load(st + 2 * SX_A, p.blk[2 * lb] + bb * SX_B, SX_B, &full[s]);
+                    bulk_load(st + 2 * SX_A + SX_B, p.blk[2 * lb + 1] + bb * SX_B, SX_B, &full[s]);
                 });
             }
         }
@@ -428,27 +356,19 @@ __device__ __forceinline__ void run_producer(const SplitParams &p, uint8_t *stag
 
 // ---------------------------------------------------------------------------
 // MMA issuer (one thread).
-template <int TYPE, int CS, int NB>
+template <int TYPE, int NB>
 __device__ __forceinline__ void run_mma(const SplitParams &p, uint8_t *stages, uint64_t *full, uint64_t *empty,
                                         uint64_t *tfull, uint64_t *tempty, uint64_t *drain, uint32_t tmem,
-                                        volatile int *abort, int rj, int rk, int64_t unit0, int64_t ustep,
-                                        const UnitRing &ring) {
-    constexpr int PJ = CS == 4 ? 2 : 1;
+                                        volatile int *abort, const UnitRing &ring) {
     constexpr int KE = TYPE == TM_F32 ? 8 : 16;
     uint32_t g = 0, sg = 0;  // stage and segment counters
     bool stop = false;
     for (int n = 0; !stop; ++n) {
-        int64_t si;
-        if (CS == 1) {
-            si = ring_take(ring, n, abort);
-            if (si == -2) stop = true;
-            if (si < 0) break;
-        } else {
-            si = unit0 + (int64_t)n * ustep;
-            if (si >= p.n_super) break;
-        }
+        const int64_t si = ring_take(ring, n, abort);
+        if (si == -2) stop = true;
+        if (si < 0) break;
         ItemBox bx;
-        decode_super<PJ>(p, si, rj, rk, bx);
+        decode_item(p, si, bx);
         for (int t = 0; t < 9 && !stop; ++t) {
             const int nk = term_chunk_count<KE>(p, bx, t);
             int kseg;
@@ -475,8 +395,7 @@ __device__ __forceinline__ void run_mma(const SplitParams &p, uint8_t *stages, u
                     mma_split<TYPE>(d_tmem, ah, bh, kc == sgi * kseg ? 0u : 1u);
                     mma_split<TYPE>(d_tmem, ah, bl, 1u);
                     mma_split<TYPE>(d_tmem, al, bh, 1u);
-                    if (CS == 4) tc::mma_commit_mc(&empty[s], 0xF);  // free here: tell all 4 CTAs
-                    else tc::mma_commit(&empty[s]);
+                    tc::mma_commit(&empty[s]);
                 }
                 if (!stop) tc::mma_commit(&tfull[buf]);  // an empty term commits nothing new
             }
@@ -760,13 +679,11 @@ __device__ __forceinline__ void write_partial(double (&e1)[NQ], double (&est)[NQ
 // TMEM accumulators; HOLD = 1: the last drain writes it to the upper 256
 // TMEM columns, which the energy warps read 32 columns at a time (their
 // registers stay free for the FP64 work), one accumulator.
-template <int TYPE, int CS, int HOLD>
+template <int TYPE, int HOLD>
 __global__ void __launch_bounds__(HOLD ? SX_THREADS_H : SX_THREADS, 1)
     split_fused_kernel(const __grid_constant__ SplitParams p) {
-    static_assert(HOLD == 0 || CS == 1, "tensor-memory hold with single CTAs only");
     constexpr int EPI = HOLD ? SX_EPI_H : SX_EPI;   // energy threads
     constexpr int NA = HOLD ? 2 : 4;                // a values per energy thread
-    constexpr int PJ = CS == 4 ? 2 : 1;
     constexpr int NB = HOLD ? 1 : 2;
     extern __shared__ __align__(1024) uint8_t smem_raw[];
     uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
@@ -793,7 +710,7 @@ __global__ void __launch_bounds__(HOLD ? SX_THREADS_H : SX_THREADS, 1)
     if (threadIdx.x == 0) {
         for (int s = 0; s < SX_NS; ++s) {
             tc::mbar_init(&full[s], 1);
-            tc::mbar_init(&empty[s], CS);  // one release from each CTA of the cluster
+            tc::mbar_init(&empty[s], 1);
         }
         for (int s = 0; s < 2; ++s) {
             tc::mbar_init(&tfull[s], 1);
@@ -815,21 +732,14 @@ __global__ void __launch_bounds__(HOLD ? SX_THREADS_H : SX_THREADS, 1)
     tc::tc_fence_before();
     __syncthreads();
     tc::tc_fence_after();
-    // every CTA's barriers exist before any peer multicasts into them
-    if (CS > 1) tc::cluster_sync();
     const uint32_t tmem = *tslot;
-    const int rank = CS > 1 ? (int)tc::cluster_rank() : 0;
-    const int rj = rank >> 1, rk = rank & 1;
-    const int64_t unit0 = CS > 1 ? tc::cluster_id_x() : blockIdx.x;
-    const int64_t ustep = CS > 1 ? tc::cluster_count_x() : gridDim.x;
 
     if (warp < 4) {
         asm volatile("setmaxnreg.dec.sync.aligned.u32 %0;" ::"n"(SX_REG_LOW));
         if (warp == 0 && lane == 0)
-            run_producer<TYPE, CS>(p, stages, full, empty, abort, rj, rk, unit0, ustep, ring);
+            run_producer<TYPE>(p, stages, full, empty, abort, ring);
         else if (warp == 1 && lane == 0)
-            run_mma<TYPE, CS, NB>(p, stages, full, empty, tfull, tempty, drain, tmem, abort, rj, rk, unit0, ustep,
-                                  ring);
+            run_mma<TYPE, NB>(p, stages, full, empty, tfull, tempty, drain, tmem, abort, ring);
     } else if (warp < 8) {
         // ---------------- drain warps ----------------
         asm volatile("setmaxnreg.dec.sync.aligned.u32 %0;" ::"n"(SX_REG_DRAIN));
@@ -841,11 +751,10 @@ __global__ void __launch_bounds__(HOLD ? SX_THREADS_H : SX_THREADS, 1)
         bool ok = true;
         for (int n = 0; ok; ++n) {
             if (leader) {
-                int64_t si = CS == 1 ? ring_take(ring, n, abort) : unit0 + (int64_t)n * ustep;
-                if (CS > 1 && si >= p.n_super) si = -1;
+                const int64_t si = ring_take(ring, n, abort);
                 if (si >= 0) {
                     ItemBox bx;
-                    decode_super<PJ>(p, si, rj, rk, bx);
+                    decode_item(p, si, bx);
                     for (int t = 0; t < 9; ++t) dr_nk[t] = term_chunk_count<KE>(p, bx, t);
                 }
                 *dr_unit = si;
@@ -925,14 +834,13 @@ __global__ void __launch_bounds__(HOLD ? SX_THREADS_H : SX_THREADS, 1)
         const int quarter0 = HOLD ? half : 2 * half;
         for (int n = 0;; ++n) {
             if (leader) {
-                int64_t si = CS == 1 ? ring_take(ring, n, abort) : unit0 + (int64_t)n * ustep;
-                if (CS > 1 && si >= p.n_super) si = -1;
+                int64_t si = ring_take(ring, n, abort);
                 bool w = si != -2;
                 if (si >= 0) {
                     w = tc::mbar_wait(xready, n & 1, kWaitNs, abort);
                     if (w) {
                         ItemBox bx;
-                        decode_super<PJ>(p, si, rj, rk, bx);
+                        decode_item(p, si, bx);
 #pragma unroll
                         for (int dd = 0; dd < 6; ++dd) {
                             desc->g[dd] = bx.start[dd] + bx.boff[dd];
@@ -987,8 +895,6 @@ __global__ void __launch_bounds__(HOLD ? SX_THREADS_H : SX_THREADS, 1)
         tc::tc_fence_after();
         tc::tmem_dealloc(tmem, 512);
     }
-    // no CTA leaves while peers may still multicast into it or arrive on its barriers
-    if (CS > 1) tc::cluster_sync();
 }
 
 // ---------------------------------------------------------------------------
@@ -1340,52 +1246,27 @@ int mixed_prepare(sdt_job *j, int type, cudaStream_t st) {
     return SDT_OK;
 }
 
-int mixed_grid(sdt_job *j, int cluster, int64_t n_super, int *grid) {
+int mixed_grid(sdt_job *j, int shape, int64_t n_items, int *grid) {
     auto setup = [&](auto kern) -> int {
         int r = cuda_check(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, SX_SMEM_ALLOC),
                            "mixed form: smem attribute");
         if (r) return r;
-        if (cluster == 4) {
-            cudaLaunchAttribute attr[1];
-            attr[0].id = cudaLaunchAttributeClusterDimension;
-            attr[0].val.clusterDim.x = 4;
-            attr[0].val.clusterDim.y = 1;
-            attr[0].val.clusterDim.z = 1;
-            cudaLaunchConfig_t cfg = {};
-            cfg.blockDim = dim3(SX_THREADS);
-            cfg.dynamicSmemBytes = SX_SMEM_ALLOC;
-            cfg.attrs = attr;
-            cfg.numAttrs = 1;
-            cfg.gridDim = dim3(4);
-            int ncl = 0;
-            r = cuda_check(cudaOccupancyMaxActiveClusters(&ncl, kern, &cfg), "mixed form: cluster occupancy");
-            if (r) return r;
-            if (ncl < 1) return fail(SDT_ERR_CUDA, "mixed form: no cluster of 4 CTAs fits on this device");
-            if (j->max_ctas > 0) ncl = std::max(1, std::min(ncl, j->max_ctas / 4));
-            *grid = (int)(4 * std::max<int64_t>(1, std::min<int64_t>(ncl, n_super)));
-        } else {
-            int nsm = 0;
-            r = cuda_check(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, j->dev), "mixed form");
-            if (r) return r;
-            if (j->max_ctas > 0) nsm = std::min(nsm, j->max_ctas);
-            *grid = (int)std::max<int64_t>(1, std::min<int64_t>(nsm, n_super));
-        }
+        int nsm = 0;
+        r = cuda_check(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, j->dev), "mixed form");
+        if (r) return r;
+        if (j->max_ctas > 0) nsm = std::min(nsm, j->max_ctas);
+        *grid = (int)std::max<int64_t>(1, std::min<int64_t>(nsm, n_items));
         return SDT_OK;
     };
     const int type = j->mixed_type;
-    if (cluster == 4) {
-        if (type == TM_F32) return setup(split_fused_kernel<TM_F32, 4, 0>);
-        if (type == TM_BF16) return setup(split_fused_kernel<TM_BF16, 4, 0>);
-        return setup(split_fused_kernel<TM_F16, 4, 0>);
+    if (shape == 2) {
+        if (type == TM_F32) return setup(split_fused_kernel<TM_F32, 1>);
+        if (type == TM_BF16) return setup(split_fused_kernel<TM_BF16, 1>);
+        return setup(split_fused_kernel<TM_F16, 1>);
     }
-    if (cluster == 2) {
-        if (type == TM_F32) return setup(split_fused_kernel<TM_F32, 1, 1>);
-        if (type == TM_BF16) return setup(split_fused_kernel<TM_BF16, 1, 1>);
-        return setup(split_fused_kernel<TM_F16, 1, 1>);
-    }
-    if (type == TM_F32) return setup(split_fused_kernel<TM_F32, 1, 0>);
-    if (type == TM_BF16) return setup(split_fused_kernel<TM_BF16, 1, 0>);
-    return setup(split_fused_kernel<TM_F16, 1, 0>);
+    if (type == TM_F32) return setup(split_fused_kernel<TM_F32, 0>);
+    if (type == TM_BF16) return setup(split_fused_kernel<TM_BF16, 0>);
+    return setup(split_fused_kernel<TM_F16, 0>);
 }
 
 int mixed_launch(sdt_job *j, const LaunchArgs &a, cudaStream_t st) {
@@ -1412,49 +1293,31 @@ int mixed_launch(sdt_job *j, const LaunchArgs &a, cudaStream_t st) {
     p.kseg = j->mixed_kseg;
     p.klist = a.klist;
     p.item_pref = a.item_pref;
-    p.super_pref = a.super_pref;
     p.factor = a.factor;
     p.n_tasks = a.n;
-    p.n_super = a.n_super;
+    p.n_items = a.items;
     p.inv_s = j->inv_s;
     p.inv_s2 = j->inv_s2;
     p.part = a.part;
     p.err = a.err;
     p.queue = a.queue;
     p.all_k = j->all_k;
+    const int threads = a.shape == 2 ? SX_THREADS_H : SX_THREADS;
     auto launch = [&](auto kern) -> int {
-        cudaLaunchAttribute attr[1];
-        attr[0].id = cudaLaunchAttributeClusterDimension;
-        attr[0].val.clusterDim.x = 4;
-        attr[0].val.clusterDim.y = 1;
-        attr[0].val.clusterDim.z = 1;
-        cudaLaunchConfig_t cfg = {};
-        cfg.blockDim = dim3(a.cluster == 2 ? SX_THREADS_H : SX_THREADS);
-        cfg.dynamicSmemBytes = SX_SMEM_ALLOC;
-        cfg.stream = st;
-        cfg.gridDim = dim3((unsigned)a.grid);
-        if (a.cluster == 4) {
-            cfg.attrs = attr;
-            cfg.numAttrs = 1;
-        }
-        int r = cuda_check(cudaLaunchKernelEx(&cfg, kern, p), "mixed form: fused kernel");
+        kern<<<(unsigned)a.grid, threads, SX_SMEM_ALLOC, st>>>(p);
         count_launch();
-        return r;
+        return cuda_check(cudaGetLastError(), "mixed form: fused kernel");
     };
     int rc = cuda_check(cudaMemsetAsync(a.queue, 0, sizeof(unsigned long long), st), "mixed form");
     if (rc) return rc;
-    if (a.cluster == 4) {
-        if (type == TM_F32) rc = launch(split_fused_kernel<TM_F32, 4, 0>);
-        else if (type == TM_BF16) rc = launch(split_fused_kernel<TM_BF16, 4, 0>);
-        else rc = launch(split_fused_kernel<TM_F16, 4, 0>);
-    } else if (a.cluster == 2) {
-        if (type == TM_F32) rc = launch(split_fused_kernel<TM_F32, 1, 1>);
-        else if (type == TM_BF16) rc = launch(split_fused_kernel<TM_BF16, 1, 1>);
-        else rc = launch(split_fused_kernel<TM_F16, 1, 1>);
+    if (a.shape == 2) {
+        if (type == TM_F32) rc = launch(split_fused_kernel<TM_F32, 1>);
+        else if (type == TM_BF16) rc = launch(split_fused_kernel<TM_BF16, 1>);
+        else rc = launch(split_fused_kernel<TM_F16, 1>);
     } else {
-        if (type == TM_F32) rc = launch(split_fused_kernel<TM_F32, 1, 0>);
-        else if (type == TM_BF16) rc = launch(split_fused_kernel<TM_BF16, 1, 0>);
-        else rc = launch(split_fused_kernel<TM_F16, 1, 0>);
+        if (type == TM_F32) rc = launch(split_fused_kernel<TM_F32, 0>);
+        else if (type == TM_BF16) rc = launch(split_fused_kernel<TM_BF16, 0>);
+        else rc = launch(split_fused_kernel<TM_F16, 0>);
     }
     return rc;
 }

@@ -145,9 +145,10 @@ class TriplesJob:
         _capi.check(self._lib.sdt_job_set_max_ctas(self._h, int(sms)), "sdt_job_set_max_ctas")
         _capi.check(self._lib.sdt_job_set_sm_exclusive(self._h, 1 if sm_exclusive else 0), "sdt_job_set_sm_exclusive")
 
-    def set_mixed_cluster(self, ctas: int) -> None:
-        """Mixed form: clusters of 1 (default) or 4 CTAs sharing operand tiles."""
-        _capi.check(self._lib.sdt_job_set_mixed_cluster(self._h, int(ctas)), "sdt_job_set_mixed_cluster")
+    def set_mixed_shape(self, shape: int) -> None:
+        """Mixed form: work-unit shape 1 (default; the finished sub-box in
+        registers) or 2 (the finished sub-box in tensor memory)."""
+        _capi.check(self._lib.sdt_job_set_mixed_shape(self._h, int(shape)), "sdt_job_set_mixed_shape")
 
     @property
     def last_kernel_ms(self) -> float:
@@ -191,20 +192,20 @@ def ccsd_t(tiling: Tiling, t1: TceFile, t2: TceFile, v2: TceFile) -> tuple[float
 class Plan:
     """A prepared evaluation of a tuple list on a job (sdt_plan_*): host
     indexing and uploads happen once; run() replays the captured CUDA graph
-    when capture() was called, else launches.  ctas (one per tuple, 1 or 4)
-    picks the mixed kernel's work-unit shape per tuple."""
+    when capture() was called, else launches.  shapes (one per tuple, 1 or
+    2) picks the mixed kernel's work-unit shape per tuple."""
 
-    def __init__(self, job: TriplesJob, klist: np.ndarray, precision: int = PREC_FP64, ctas=None):
+    def __init__(self, job: TriplesJob, klist: np.ndarray, precision: int = PREC_FP64, shapes=None):
         self.job = job
         self._lib = job._lib
         self.klist = np.ascontiguousarray(klist, dtype=np.int64).reshape(-1, 7)
-        self.ctas = None if ctas is None else np.ascontiguousarray(ctas, dtype=np.int32)
-        if self.ctas is not None and len(self.ctas) != len(self.klist):
-            raise ValueError("one cluster size per tuple")
+        self.shapes = None if shapes is None else np.ascontiguousarray(shapes, dtype=np.int32)
+        if self.shapes is not None and len(self.shapes) != len(self.klist):
+            raise ValueError("one work-unit shape per tuple")
         h = C.c_void_p()
         _capi.check(self._lib.sdt_plan_create(
             job._h, self.klist.ctypes.data_as(_capi.PI64), len(self.klist), int(precision),
-            None if self.ctas is None else self.ctas.ctypes.data_as(C.POINTER(C.c_int32)), C.byref(h)),
+            None if self.shapes is None else self.shapes.ctypes.data_as(C.POINTER(C.c_int32)), C.byref(h)),
             "sdt_plan_create")
         self._h = h
         self.precision = int(precision)

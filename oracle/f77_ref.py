@@ -13,6 +13,9 @@ goes to oracle/_ref/, which is not committed.
 
     python oracle/f77_ref.py [NWCHEM_SOURCE_TREE]
 
+The tree is the argument, else the NWCHEM_SRC environment variable, else
+the location this build's container mounts it at.
+
 Preprocessing: the files are run through the C preprocessor in traditional
 mode with no macros defined, which takes the reference's generic branches
 (not CRAYFTN, not __ppc64__, no OpenMP directives; OpenMP directives are
@@ -20,6 +23,7 @@ comment lines in any case).
 """
 from __future__ import annotations
 
+import os
 import re
 import subprocess
 import sys
@@ -27,7 +31,7 @@ from pathlib import Path
 
 HERE = Path(__file__).resolve().parent
 OUT = HERE / "_ref"
-DEFAULT_TREE = Path("/root/reference")
+DEFAULT_TREE = Path(os.environ.get("NWCHEM_SRC", "/root/reference"))
 FILES = ["src/tce/ccsd_t/ccsd_t_kernels_omp.F", "src/tce/ccsd_t/ccsd_t_dot.F"]
 
 

@@ -1,8 +1,10 @@
 """Regenerates tests/golden/reference_kernels.json from the reference's own code.
 
-Run from the repository root (needs the NWChem source tree at /root/reference):
+Run from the repository root; it needs the NWChem source tree (the
+argument, else the NWCHEM_SRC environment variable, as oracle/f77_ref.py
+takes it):
 
-    python tests/golden/make_ref_golden.py
+    python tests/golden/make_ref_golden.py [NWCHEM_SOURCE_TREE]
 
 It builds oracle/_ref/libref_kernels.so with oracle/f77_ref.py -- a
 statement-by-statement translation of src/tce/ccsd_t/ccsd_t_kernels_omp.F
@@ -57,7 +59,7 @@ def dot_inputs(case, seed: int):
 
 
 def main() -> None:
-    lib = C.CDLL(str(f77_ref.build()))
+    lib = C.CDLL(str(f77_ref.build(Path(sys.argv[1]) if len(sys.argv) > 1 else f77_ref.DEFAULT_TREE)))
     i64 = lambda v: C.byref(C.c_int64(int(v)))
     pd = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))
     out = {"source": "translated from src/tce/ccsd_t/ccsd_t_kernels_omp.F and ccsd_t_dot.F by oracle/f77_ref.py",

@@ -27,22 +27,22 @@ def test_choices_are_the_cheapest_and_cached(tmp_path):
     t, kl = _setup()
     calls = []
 
-    def fake(sub, precision, ctas):
-        calls.append((len(sub), precision, ctas))
-        # fp16 fastest; clusters of 4 pay off only for the biggest class
+    def fake(sub, precision, shape):
+        calls.append((len(sub), precision, shape))
+        # fp16 fastest; the tensor-memory hold shape pays off only for the biggest class
         base = {ng.PREC_MIXED_FP16: 1.0, ng.PREC_MIXED_BF16: 1.1, ng.PREC_MIXED_TF32: 2.0}[precision]
         big = max(autotune.size_class(t, k) for k in sub) == max(autotune.size_class(t, k) for k in kl)
-        return ng.flops(t, sub) * base * (0.9 if (ctas == 4 and big) else 1.0)
+        return ng.flops(t, sub) * base * (0.9 if (shape == 2 and big) else 1.0)
 
     cache = tmp_path / "tune.json"
     tuner = autotune.Autotuner(SimpleNamespace(tiling=t), cache=cache, measure=fake, sample=3)
     d = tuner.tune(kl)
     assert d["form"] == "fp16"
     top = max(tuner.classes(kl))
-    assert all(v == (4 if c == top else 1) for c, v in d["shapes"].items())
+    assert all(v == (2 if c == top else 1) for c, v in d["shapes"].items())
     assert cache.exists() and calls
-    ctas = tuner.ctas(kl, d)
-    assert ctas.shape == (len(kl),) and set(ctas.tolist()) <= {1, 2, 4}
+    shapes = tuner.shapes(kl, d)
+    assert shapes.shape == (len(kl),) and set(shapes.tolist()) <= {1, 2}
     # a second tuner reuses the cache without timing anything
     calls.clear()
     again = autotune.Autotuner(SimpleNamespace(tiling=t), cache=cache, measure=fake).tune(kl)
@@ -51,6 +51,6 @@ def test_choices_are_the_cheapest_and_cached(tmp_path):
 
 def test_forms_restrict_the_split_choice():
     t, kl = _setup()
-    fake = lambda sub, prec, ctas: {ng.PREC_MIXED_BF16: 1.0}.get(prec, 5.0)
+    fake = lambda sub, prec, shape: {ng.PREC_MIXED_BF16: 1.0}.get(prec, 5.0)
     d = autotune.Autotuner(SimpleNamespace(tiling=t), forms=("tf32", "fp16"), measure=fake).tune(kl)
     assert d["form"] in ("tf32", "fp16")

@@ -160,12 +160,10 @@ def test_mixed_persistent_many_items(cuda_device):
             assert m[0] == pytest.approx(f[0], rel=b) and m[1] == pytest.approx(f[1], rel=b)
 
 
-@pytest.mark.parametrize("shape", [2, 4])
 @pytest.mark.parametrize("form", ["fp16", "tf32"])
-def test_mixed_work_unit_shapes(cuda_device, form, shape):
-    """Clusters of 4 CTAs (multicast operand tiles, (j,k) box pairs, odd box
-    counts leave idle CTAs) and single CTAs holding the finished sub-box in
-    tensor memory give the same bits as single CTAs."""
+def test_mixed_work_unit_shapes(cuda_device, form):
+    """CTAs holding the finished sub-box in tensor memory give the same bits
+    as CTAs holding it in registers."""
     import nwchem_gb300 as ng
     t = ng.Tiling([3, 5, 6], [9, 6, 10, 17]).with_evl(8)
     files = ng.synth_inputs(t, 8)
@@ -174,7 +172,7 @@ def test_mixed_work_unit_shapes(cuda_device, form, shape):
         job.load(*files)
         f = job.run(kl)
         a = job.run(kl, per_task=True, precision=PREC[form])
-        job.set_mixed_cluster(shape)
+        job.set_mixed_shape(2)
         b = job.run(kl, per_task=True, precision=PREC[form])
     assert a[0] == b[0] and a[1] == b[1] and np.array_equal(a[2], b[2])
     bnd = MIXED_BOUND[form]

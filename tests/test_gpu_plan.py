@@ -45,13 +45,12 @@ def test_plan_matches_job_run_and_graph_replays(sym_job, prec):
 
 
 def test_plan_per_tuple_shapes(sym_job):
-    """Tuples split between single CTAs, single CTAs holding the sub-box in
-    tensor memory and clusters of 4 give each tuple's bits of the single-CTA
-    run, in the caller's order."""
+    """Tuples split between the register-hold and the tensor-memory-hold
+    shapes give each tuple's bits of the register-hold run, in the caller's
+    order."""
     t, job, kl = sym_job
-    ctas = \
-        np.array([[4, 1, 2][q % 3] for q in range(len(kl))], dtype=np.int32)
-    with ng.Plan(job, kl, ng.PREC_MIXED_FP16) as p1, ng.Plan(job, kl, ng.PREC_MIXED_FP16, ctas) as p2:
+    shapes = np.array([[2, 1, 2][q % 3] for q in range(len(kl))], dtype=np.int32)
+    with ng.Plan(job, kl, ng.PREC_MIXED_FP16) as p1, ng.Plan(job, kl, ng.PREC_MIXED_FP16, shapes) as p2:
         a = p1.run(per_task=True)
         p2.capture()
         b = p2.run(per_task=True)
@@ -77,6 +76,6 @@ def test_autotuned_plan(sym_job, tmp_path):
     with p:
         e = p.run()
         e2 = p.run()
-    assert d["form"] in ("fp16", "tf32") and set(d["shapes"].values()) <= {1, 2, 4}
+    assert d["form"] in ("fp16", "tf32") and set(d["shapes"].values()) <= {1, 2}
     assert e == e2
     assert e[0] == pytest.approx(f[0], rel=2e-6) and e[1] == pytest.approx(f[1], rel=2e-6)

@@ -2,7 +2,9 @@
 own the triples tiles in their own device memory and cannot allocate
 (a memory pool that already holds the budget, or device data owned by a
 Fortran offload runtime).  It must give compute_en_'s energies for the same
-tiles, on two calls in a row (the fixed scratch array is reused)."""
+tiles, on two calls in a row (the fixed scratch array is reused), and the
+device's free memory (cudaMemGetInfo) must not move across its calls once
+the first call has loaded the library's module."""
 import ctypes as C
 
 import numpy as np
@@ -57,12 +59,21 @@ def test_noalloc_energy_matches_compute_en_twice(cuda_device):
         d_dev = torch.from_numpy(d_host).to(cuda_device)
         s_dev = torch.from_numpy(s_host).to(cuda_device)
         torch.cuda.synchronize()
+        # The first call in a process may load the library's module (and its
+        # fixed array); after that, free device memory must stay put.
+        free0 = torch.cuda.mem_get_info(cuda_device)[0] if q > 0 else None
         for _ in range(2):
             got = np.full(2, np.nan)
             rc = lib.sdt_compute_en_noalloc(f, _pd(got), *[_pd(x) for x in ev], *td,
                                             C.c_void_p(d_dev.data_ptr()), C.c_void_p(s_dev.data_ptr()),
                                             None)
             _capi.check(rc, "sdt_compute_en_noalloc")
+            torch.cuda.synchronize()
+            free = torch.cuda.mem_get_info(cuda_device)[0]
+            if free0 is None:
+                free0 = free                             # after the first call (module loaded)
+            else:
+                assert free == free0, f"free device memory moved by {free - free0} bytes"
             assert got[0] == pytest.approx(ref[0], rel=1e-12, abs=1e-300)
             assert got[1] == pytest.approx(ref[1], rel=1e-12, abs=1e-300)
 
