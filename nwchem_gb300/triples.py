@@ -52,8 +52,10 @@ class TceFile:
         return -1
 
 
-def synth_file(tiling: Tiling, kind: int, seed: int, pinned: bool = False) -> TceFile:
-    """Seeded synthetic TCE file (T1, T2 or V2 with its vvov, ovoo and vvoo blocks)."""
+def synth_file(tiling: Tiling, kind: int, seed: int, pinned: bool = False, scale: float = 1.0) -> TceFile:
+    """Seeded synthetic TCE file (T1, T2 or V2 with its vvov, ovoo and vvoo
+    blocks), every element multiplied by `scale` (amplitudes and integrals
+    scaled by s scale both energies by s**4)."""
     lib = _capi.lib()
     ts = tiling.struct()
     nb, nd = C.c_int64(), C.c_int64()
@@ -68,11 +70,22 @@ def synth_file(tiling: Tiling, kind: int, seed: int, pinned: bool = False) -> Tc
     _capi.check(lib.sdt_synth_file(C.byref(ts), kind, seed, C.byref(nb), C.byref(nd),
                                    h.ctypes.data_as(_capi.PI64), d.ctypes.data_as(_capi.PD)),
                 "sdt_synth_file")
+    if scale != 1.0:
+        d *= scale
     return TceFile(h, d)
 
 
-def synth_inputs(tiling: Tiling, seed: int, pinned: bool = False) -> tuple[TceFile, TceFile, TceFile]:
-    return tuple(synth_file(tiling, k, seed, pinned) for k in (FILE_T1, FILE_T2, FILE_V2))
+def synth_inputs(tiling: Tiling, seed: int, pinned: bool = False,
+                 scale: float = 1.0) -> tuple[TceFile, TceFile, TceFile]:
+    """The seeded T1, T2 and V2 files; `scale` multiplies every element (the
+    energies scale by scale**4, which brings the synthetic E(T) of many Eh
+    to the tens of mEh of a molecule)."""
+    return tuple(synth_file(tiling, k, seed, pinned, scale) for k in (FILE_T1, FILE_T2, FILE_V2))
+
+
+def molecular_scale(e_t: float, target: float = 0.05) -> float:
+    """The input scale that maps a synthetic E(T) of e_t Eh to |E(T)| = target."""
+    return (target / abs(e_t)) ** 0.25 if e_t else 1.0
 
 
 def task_list(tiling: Tiling) -> np.ndarray:

@@ -79,6 +79,12 @@ def lib():
             _lib.orc_tce_sort_2.argtypes = [PD, PD] + [I64] * 4 + [C.c_double]
             _lib.orc_tce_hash.restype = I64
             _lib.orc_tce_hash.argtypes = [PI64, I64]
+            _lib.orc_synth_evl.restype = None
+            _lib.orc_synth_evl.argtypes = [I64, I64, C.c_uint64, PD]
+            _lib.orc_synth_file.restype = I64
+            _lib.orc_synth_file.argtypes = [C.POINTER(OrcTiling), C.c_int, C.c_uint64, PI64, PI64, PI64, PD]
+            _lib.orc_tasks_flops.restype = C.c_double
+            _lib.orc_tasks_flops.argtypes = [C.POINTER(OrcTiling), PI64, I64]
         return _lib
 
 
@@ -161,6 +167,79 @@ class Problem:
         if rc != 0:
             raise RuntimeError(f"orc_tuple_drive failed ({rc})")
         return calls
+
+
+class Tiling:
+    """A tiling with the attributes Problem reads (spin-orbital, unrestricted,
+    irreps optional), built without the product library."""
+
+    def __init__(self, occ, vir, occ_sym=None, vir_sym=None, seed: int = 0, name: str = "custom"):
+        self.occ, self.vir, self.name = [int(x) for x in occ], [int(x) for x in vir], name
+        self.noab, self.nvab = len(self.occ), len(self.vir)
+        self.range = np.array(self.occ + self.vir, dtype=np.int64)
+        self.spin = np.ones(self.noab + self.nvab, dtype=np.int64)
+        self.sym = np.array(list(occ_sym or [0] * self.noab) + list(vir_sym or [0] * self.nvab), dtype=np.int64)
+        self.offset = np.concatenate([[0], np.cumsum(self.range)[:-1]]).astype(np.int64)
+        self.alpha_arr, self.restricted = None, False
+        self.nocc, self.nvir = int(sum(self.occ)), int(sum(self.vir))
+        self.evl = np.empty(self.nocc + self.nvir)
+        lib().orc_synth_evl(self.nocc, self.nvir, seed, _pd(self.evl))
+        self._ts = OrcTiling(self.noab, self.nvab, _pi(self.range), _pi(self.spin), _pi(self.sym),
+                             _pi(self.offset), C.cast(None, PI64), _pd(self.evl), 0, 0, 0)
+
+
+def config_tiling(config: int) -> Tiling:
+    """The benchmark workloads' tilings, with their seeded orbital energies:
+    0 o=10/v=40 one tile each; 1 o=40 as 8/12/20, v=300 as 20,24x5,30x4,40;
+    2 o=64 as 2x32, v=512 as 8x64; 3 blocked symmetry, 8 occupied tiles
+    (irreps 0..7) from {8,12,16,24,32} and 12 virtual tiles (irreps
+    0..7,0..3) from {16,24,32,48,64}, drawn by numpy's PCG64 with seed 3."""
+    if config == 0:
+        return Tiling([10], [40], seed=0, name="o10v40")
+    if config == 1:
+        return Tiling([8, 12, 20], [20, 24, 24, 24, 24, 24, 30, 30, 30, 30, 40], seed=1, name="o40v300")
+    if config == 2:
+        return Tiling([32, 32], [64] * 8, seed=2, name="o64v512")
+    if config == 3:
+        rng = np.random.default_rng(3)
+        occ = [int(x) for x in rng.choice([8, 12, 16, 24, 32], 8)]
+        vir = [int(x) for x in rng.choice([16, 24, 32, 48, 64], 12)]
+        return Tiling(occ, vir, [q % 8 for q in range(8)], [q % 8 for q in range(12)], seed=3,
+                      name="sym8_o%dv%d" % (sum(occ), sum(vir)))
+    raise ValueError(f"no tiling for workload {config}")
+
+
+class File:
+    """One TCE file: tce_hash table and block data."""
+
+    def __init__(self, hash_: np.ndarray, data: np.ndarray):
+        self.hash, self.data = hash_, data
+
+    @property
+    def nbytes(self) -> int:
+        return int(self.hash.nbytes + self.data.nbytes)
+
+
+def synth_inputs(tiling: Tiling, seed: int) -> tuple[File, File, File]:
+    """The workloads' seeded T1, T2 and V2 files (orc_synth.c)."""
+    L, out = lib(), []
+    for kind in range(3):
+        nb, nd = C.c_int64(), C.c_int64()
+        if L.orc_synth_file(C.byref(tiling._ts), kind, seed, C.byref(nb), C.byref(nd), None, None) != 0:
+            raise RuntimeError("orc_synth_file failed")
+        h, d = np.empty(2 * nb.value + 1, dtype=np.int64), np.empty(nd.value)
+        if L.orc_synth_file(C.byref(tiling._ts), kind, seed, C.byref(nb), C.byref(nd), _pi(h), _pd(d)) != 0:
+            raise RuntimeError("orc_synth_file failed")
+        out.append(File(h, d))
+    return tuple(out)
+
+
+def flops(tiling, klist: np.ndarray) -> float:
+    """Algorithmic FLOPs of a tuple list (orc_tasks_flops)."""
+    kl = np.ascontiguousarray(klist, dtype=np.int64).reshape(-1, 7)
+    p = Problem.__new__(Problem)
+    Problem.__init__(p, tiling, *(File(np.zeros(1, dtype=np.int64), np.zeros(1)),) * 3)
+    return float(lib().orc_tasks_flops(C.byref(p.ts), _pi(kl), len(kl)))
 
 
 def kernel(family: str, k: int, dims_fortran, triplesx: np.ndarray, a: np.ndarray, b: np.ndarray) -> None:

@@ -140,6 +140,17 @@ int64_t orc_tuple_tiles(const orc_tiling *t, const orc_file *t1,
                         const int64_t *tuple6, double *singles,
                         double *doubles);
 
+/* ---- synthetic workload inputs (orc_synth.c) ----------------------------
+ * The benchmark workloads' seeded inputs on the checker side, byte for byte
+ * the library's sdt_synth_file / sdt_synth_evl, so that the CPU baseline
+ * runs without the product library.  kind: 0 T1, 1 T2, 2 V2.  With hash or
+ * data NULL only the counts are returned.  0 on success. */
+void orc_synth_evl(int64_t nocc, int64_t nvir, uint64_t seed, double *evl);
+int64_t orc_synth_file(const orc_tiling *t, int kind, uint64_t seed, int64_t *nblocks, int64_t *ndata,
+                       int64_t *hash, double *data);
+/* Algorithmic FLOPs of a tuple list (7 entries per tuple). */
+double orc_tasks_flops(const orc_tiling *t, const int64_t *klist, int64_t n);
+
 #ifdef __cplusplus
 }
 #endif

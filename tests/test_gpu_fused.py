@@ -76,21 +76,67 @@ def test_fused_workload0(gpu):
     assert (e2 - e1) == pytest.approx(g["E[ST]"], rel=1e-8, abs=0)
 
 
-def test_fused_workload1_sampled_tuples(gpu):
-    """o=40 (8/12/20), v=300 (11 tiles): per-tuple energies of a seeded
-    sample of tuples against the oracle."""
+def _across_sizes(t, kl, rng, quantiles, extra=()):
+    """Tuple indices at the given quantiles of the per-tuple FLOP count
+    (seeded pick inside a narrow band around each), plus `extra`."""
+    fl = np.array([ng.flops(t, kl[q:q + 1]) for q in range(len(kl))])
+    order = np.argsort(fl, kind="stable")
+    n = len(order)
+    ids = []
+    for qt in quantiles:
+        lo, hi = int(qt * (n - 1)), min(n, int(qt * (n - 1)) + max(1, n // 50))
+        ids.append(int(order[rng.integers(lo, hi)]))
+    ids.extend(int(x) for x in extra)
+    return np.unique(np.array(ids, dtype=np.int64)), fl
+
+
+def _diagonal(k):
+    return k[0] == k[1] or k[1] == k[2] or k[3] == k[4] or k[4] == k[5]
+
+
+def test_fused_workload1_tuples_across_sizes(gpu):
+    """o=40 (8/12/20), v=300 (11 tiles), seed 1: per-tuple energies of
+    tuples drawn from every part of the size range (5 %, 25 %, 50 %, 75 %,
+    95 % FLOP quantiles), the heaviest tuple of the 2860 (40x40x40x20x20x20,
+    5.1e8 triples elements) and one tuple with no repeated tile, FP64 against
+    the oracle at 1e-10 and each mixed form within its bound."""
     t = ng.config_tiling(1)
     files = ng.synth_inputs(t, 1)
     kl = ng.task_list(t)
-    rng = np.random.default_rng(1)
-    small = np.argsort(kl[:, 6])[:40]           # the oracle finishes these in seconds
-    ids = np.sort(rng.choice(small, 5, replace=False))
+    rng = np.random.default_rng(101)
+    plain = [q for q in range(len(kl)) if not _diagonal(kl[q])]
+    ids, fl = _across_sizes(t, kl, rng, (0.05, 0.25, 0.5, 0.75, 0.95), extra=(plain[len(plain) // 2],))
+    ids = np.unique(np.append(ids, int(np.argmax(fl))))
+    assert any(_diagonal(kl[q]) for q in ids) and any(not _diagonal(kl[q]) for q in ids)
     P = orc.Problem(t, *files)
     _, _, pt, _ = P.ccsd_t(kl, task_ids=ids)
     with ng.TriplesJob(t) as job:
         job.load(*files)
         _, _, gpt = job.run(kl[ids], per_task=True)
+        mixed = {f: job.run(kl[ids], per_task=True, precision=p)[2] for f, p in (("tf32", 1), ("bf16", 2), ("fp16", 3))}
     assert np.allclose(gpt, pt, rtol=REL, atol=0)
+    bound = {"tf32": 2e-5, "fp16": 2e-5, "bf16": 5e-5}   # per tuple: fewer elements than a whole job
+    for f, m in mixed.items():
+        assert np.all(np.abs(m - pt) <= bound[f] * np.abs(pt)), f
+
+
+def test_fused_workload3_tuples_across_sizes(gpu):
+    """Blocked spatial symmetry (8 irreps, the first 4096 tuples of its weight
+    order, seed 3): per-tuple energies of the workload's own tuples at the
+    10/30/50/70/90 % FLOP quantiles, FP64 against the oracle at 1e-10 and
+    FP16x3 within its bound."""
+    t = ng.config_tiling(3)
+    files = ng.synth_inputs(t, 3)
+    kl = ng.task_list(t)[:4096]
+    ids, _ = _across_sizes(t, kl, np.random.default_rng(103), (0.1, 0.3, 0.5, 0.7, 0.9))
+    P = orc.Problem(t, *files)
+    _, _, pt, _ = P.ccsd_t(kl, task_ids=ids)
+    with ng.TriplesJob(t) as job:
+        job.load(*files)
+        _, _, gpt = job.run(kl[ids], per_task=True)
+        _, _, mpt = job.run(kl[ids], per_task=True, precision=ng.PREC_MIXED_FP16)
+    assert np.allclose(gpt, pt, rtol=REL, atol=0)
+    assert np.all(np.abs(mpt - pt) <= 2e-5 * np.abs(pt))
 
 
 def test_fused_deterministic(gpu):

@@ -152,3 +152,35 @@ def test_restricted_mapping_reads_alpha_blocks():
     e1, e2, _, kc = P.ccsd_t()
     assert np.isfinite(e1) and e1 < 0
     assert len(kc) == len(ng.task_list(t))
+
+
+def test_oracle_workload_inputs_equal_the_library():
+    """The checker-side generator (orc_synth.c), tilings, tuple lists and
+    FLOP counts are byte for byte the library's, and the o=10/v=40 files
+    match the committed digests: the CPU baseline runs on the same inputs
+    without loading the product library."""
+    import hashlib
+    import json
+    from pathlib import Path
+    gold = json.loads((Path(__file__).resolve().parent / "golden" / "oracle_known_answers.json").read_text())
+    for c in (0, 1, 3):
+        a, b = orc.config_tiling(c), ng.config_tiling(c)
+        assert np.array_equal(a.range, b.range) and np.array_equal(a.sym, b.sym)
+        assert np.array_equal(a.evl, b.evl)
+        fa = orc.synth_inputs(a, c)
+        if c == 0:
+            for name, f in zip(("T1", "T2", "V2"), fa):
+                d = gold["synth_sha256"][f"o10v40_seed0_{name}"]
+                assert hashlib.sha256(f.hash.tobytes()).hexdigest() == d["hash"]
+                assert hashlib.sha256(f.data.tobytes()).hexdigest() == d["data"]
+        if c != 1:   # o=40/v=300: 5.7 GB, compared through the tuple list only
+            fb = ng.synth_inputs(b, c)
+            for x, y in zip(fa, fb):
+                assert np.array_equal(x.hash, y.hash) and np.array_equal(x.data, y.data)
+        kl = orc.Problem(a, *fa).task_list()
+        assert np.array_equal(kl, ng.task_list(b))
+        assert orc.flops(a, kl) == ng.flops(b, kl)
+    t = ng.Tiling([3, 2, 3], [4, 5, 4, 3], occ_sym=[0, 1, 1], vir_sym=[1, 0, 1, 0]).with_evl(5)
+    o = orc.Tiling([3, 2, 3], [4, 5, 4, 3], [0, 1, 1], [1, 0, 1, 0], seed=5)
+    for x, y in zip(orc.synth_inputs(o, 5), ng.synth_inputs(t, 5)):
+        assert np.array_equal(x.hash, y.hash) and np.array_equal(x.data, y.data)
