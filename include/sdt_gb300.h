@@ -264,15 +264,19 @@ int sdt_plan_destroy(sdt_plan *plan);
 int64_t sdt_plan_items(const sdt_plan *plan);
 
 /* Serving (no reference counterpart): a loop of independent (T) jobs on
- * one GPU.  Jobs wait in one FIFO queue and are admitted when one of
- * `slots` workers is free and sdt_job_bytes of the job fits in the byte
+ * one GPU.  Jobs wait in one FIFO queue and are admitted when fewer than
+ * `slots` jobs are in flight and sdt_job_bytes of the job fits in the byte
  * budget minus the admitted jobs' bytes (a job larger than the budget
- * fails with SDT_ERR_NOMEM); each admitted job runs on its own stream --
- * create, load, the given precision over all its tuples -- so admitted
- * jobs overlap on the device.  A job submitted with check_fp64 keeps its
- * device memory after its energies are delivered (state 3) and runs the
- * FP64 form as a check when no admissible job is waiting.
- * max_ctas (0: all SMs) caps the CTAs of each job's persistent launches.
+ * fails with SDT_ERR_NOMEM); `slots` workers load admitted jobs, each on
+ * its own stream.  Continuous batching: jobs of the server's mixed form
+ * (FP16x3 unless sdt_server_set_queue says otherwise) have their sub-box
+ * items appended to one device work queue that a resident persistent
+ * kernel drains while they arrive; it keeps `reserve` SMs free for loading
+ * and finishing other jobs, and each job's energies are delivered when its
+ * last item is done.  Jobs of other precisions run their own launches
+ * (max_ctas, 0: all SMs, caps those).  A job submitted with check_fp64
+ * keeps its device memory after its energies are delivered (state 3) and
+ * runs the FP64 form as a check when no admissible job is waiting.
  * The caller keeps a job's files alive until its state is 2 (done) or -1
  * (failed).  Times are seconds since sdt_server_create. */
 typedef struct sdt_server sdt_server;
@@ -290,9 +294,24 @@ int sdt_server_submit(sdt_server *server, const sdt_tiling *t,
 int sdt_server_status(sdt_server *server, int64_t ticket, int *state,
                       double *energy, double *fp64, double *times,
                       char *msg, size_t len);
-/* CTAs of each deferred FP64 check (default a quarter of the SMs); while a
- * check runs, mixed jobs launch on the remaining SMs.  0: no cap. */
+/* CTAs (one per SM) of each deferred FP64 check (default half the SMs the
+ * shared queue leaves free, or a quarter of the SMs without the queue). */
 int sdt_server_set_check_ctas(sdt_server *server, int ctas);
+/* The shared queue: its precision (SDT_PREC_FP64 turns it off), work-unit
+ * shape (1 or 2, as sdt_job_set_mixed_shape; default 2), SMs kept free of
+ * the resident kernel (default 16) and the seconds (at most 1) the kernel
+ * waits for new work before it leaves (default 0.2).  Before the first
+ * submit. */
+int sdt_server_set_queue(sdt_server *server, int precision, int shape,
+                         int reserve_sms, double idle_s);
+/* stats[4]: resident-kernel launches, jobs that went through the queue,
+ * most jobs in the queue at once, jobs in it now. */
+int sdt_server_queue_stats(sdt_server *server, int64_t *stats);
+/* The resident-kernel launches (numbered from 1) that took the job's first
+ * item and finished its last item; 0 when the job did not go through the
+ * queue or has not finished. */
+int sdt_server_job_launches(sdt_server *server, int64_t ticket, int *first,
+                            int *last);
 /* Cancels a queued job (state -1, SDT_ERR_STATE); an admitted job is not
  * stopped (SDT_ERR_STATE is returned). */
 int sdt_server_cancel(sdt_server *server, int64_t ticket);

@@ -52,6 +52,8 @@ struct sdt_job {
 
 
 namespace sdt {
+// Returns SDT_OK or records a CUDA error with context.
+int cuda_check(cudaError_t e, const char *what);
 // Multiplicity factor of a tuple (ccsd_t_dot.F:52-66).
 double tuple_factor(const int64_t *k, bool restricted);
 
@@ -82,4 +84,34 @@ int mixed_prepare(sdt_job *j, int type, cudaStream_t st);
 // kernel's shared-memory attribute; call outside stream capture).
 int mixed_grid(sdt_job *j, int shape, int64_t n_items, int *grid);
 int mixed_launch(sdt_job *j, const LaunchArgs &a, cudaStream_t st);
+
+// The shared item queue of the serving path (device buffers owned by the
+// caller; see QueueCtl in sdt_split.cu for the protocol).  table holds
+// max_jobs entries of mixed_job_entry_bytes() each.
+struct QueueArgs {
+    const void *table = nullptr;
+    const long long *base = nullptr;
+    unsigned long long *head = nullptr;
+    const unsigned long long *tail = nullptr;
+    unsigned long long *done = nullptr;
+    int *first_gen = nullptr, *last_gen = nullptr;  // host-mapped
+    const int *close = nullptr;
+    int *err = nullptr;
+    unsigned long long idle_ns = 0;
+    int max_jobs = 0, gen = 0;
+};
+size_t mixed_job_entry_bytes();
+// Writes the queue-table entry of a plan group of job j (prepared split operands).
+int mixed_job_entry(sdt_job *j, const LaunchArgs &a, void *entry);
+// Sets the queue kernel's shared-memory attribute (outside stream capture).
+int mixed_queue_prepare(int type, int shape);
+int mixed_queue_launch(int type, int shape, const QueueArgs &a, int grid, cudaStream_t st);
+
+// Plans, for the serving queue: create; the queue-table entry of a mixed
+// plan of one work-unit shape (and its item count); the sums and read-back
+// of its energies once every item pair is written; free.
+int plan_make(sdt_job *j, const int64_t *klist, int64_t n, int precision, const int32_t *shapes, sdt_plan **out);
+int plan_queue_entry(sdt_plan *p, void *entry, int64_t *items);
+int plan_finish(sdt_plan *p, cudaStream_t st, double *energy);
+void plan_release(sdt_plan *p);
 }  // namespace sdt

@@ -178,6 +178,35 @@ int plan_create(sdt_job *j, const int64_t *klist, int64_t n, int precision, cons
     return SDT_OK;
 }
 
+LaunchArgs group_args(sdt_plan *p, size_t gi) {
+    const auto &g = p->groups[gi];
+    LaunchArgs a;
+    a.klist = p->klist_d + 7 * g.t0;
+    a.item_pref = p->rpref_d + g.t0 + gi;
+    a.factor = p->factor_d + g.t0;
+    a.part = p->part_d + 2 * g.i0;
+    a.n = g.t1 - g.t0;
+    a.items = g.items;
+    a.queue = p->queue_d + gi;
+    a.err = p->err_d;
+    a.shape = g.shape;
+    a.grid = g.grid;
+    return a;
+}
+
+// The per-tuple and total sums of the plan's item pairs and their copy to
+// pinned host memory.
+int plan_sums(sdt_plan *p, cudaStream_t st) {
+    int rc = tuple_sums(p->part_d, p->gpref_d, p->n, p->task_d, p->out_d, st);
+    if (!rc) rc = cuda_check(cudaMemcpyAsync(p->host_out, p->out_d, 2 * sizeof(double), cudaMemcpyDeviceToHost, st),
+                             "sdt_plan_launch");
+    if (!rc) rc = cuda_check(cudaMemcpyAsync(p->host_out + 2, p->task_d, 2 * p->n * sizeof(double),
+                                             cudaMemcpyDeviceToHost, st), "sdt_plan_launch");
+    if (!rc) rc = cuda_check(cudaMemcpyAsync(p->err_h, p->err_d, sizeof(int), cudaMemcpyDeviceToHost, st),
+                             "sdt_plan_launch");
+    return rc;
+}
+
 // Enqueues one evaluation (device work only).
 int plan_enqueue(sdt_plan *p, cudaStream_t st) {
     sdt_job *j = p->job;
@@ -197,28 +226,11 @@ int plan_enqueue(sdt_plan *p, cudaStream_t st) {
     if (timed && !rc) rc = cuda_check(cudaEventRecordWithFlags(j->ev0, st, evflag), "sdt_plan_launch");
     if (rc) return rc;
     for (size_t gi = 0; gi < p->groups.size() && !rc; ++gi) {
-        const auto &g = p->groups[gi];
-        LaunchArgs a;
-        a.klist = p->klist_d + 7 * g.t0;
-        a.item_pref = p->rpref_d + g.t0 + gi;
-        a.factor = p->factor_d + g.t0;
-        a.part = p->part_d + 2 * g.i0;
-        a.n = g.t1 - g.t0;
-        a.items = g.items;
-        a.queue = p->queue_d + gi;
-        a.err = p->err_d;
-        a.shape = g.shape;
-        a.grid = g.grid;
+        const LaunchArgs a = group_args(p, gi);
         rc = p->mtype >= 0 ? mixed_launch(j, a, st) : fp64_launch(j, a, st);
     }
     if (timed && !rc) rc = cuda_check(cudaEventRecordWithFlags(j->ev1, st, evflag), "sdt_plan_launch");
-    if (!rc) rc = tuple_sums(p->part_d, p->gpref_d, p->n, p->task_d, p->out_d, st);
-    if (!rc) rc = cuda_check(cudaMemcpyAsync(p->host_out, p->out_d, 2 * sizeof(double), cudaMemcpyDeviceToHost, st),
-                             "sdt_plan_launch");
-    if (!rc) rc = cuda_check(cudaMemcpyAsync(p->host_out + 2, p->task_d, 2 * p->n * sizeof(double),
-                                             cudaMemcpyDeviceToHost, st), "sdt_plan_launch");
-    if (!rc) rc = cuda_check(cudaMemcpyAsync(p->err_h, p->err_d, sizeof(int), cudaMemcpyDeviceToHost, st),
-                             "sdt_plan_launch");
+    if (!rc) rc = plan_sums(p, st);
     return rc;
 }
 
@@ -244,6 +256,30 @@ int plan_read(sdt_plan *p, cudaStream_t st, double *energy, double *per_task, co
 }
 
 }  // namespace
+
+int plan_make(sdt_job *j, const int64_t *klist, int64_t n, int precision, const int32_t *shapes, sdt_plan **out) {
+    return plan_create(j, klist, n, precision, shapes, out, "sdt_plan_create");
+}
+
+int plan_queue_entry(sdt_plan *p, void *entry, int64_t *items) {
+    if (p->mtype < 0 || p->groups.size() != 1)
+        return fail(SDT_ERR_ARG, "queue entry: a mixed-form plan of one work-unit shape is needed");
+    *items = p->items;
+    return mixed_job_entry(p->job, group_args(p, 0), entry);
+}
+
+int plan_finish(sdt_plan *p, cudaStream_t st, double *energy) {
+    if (p->n == 0) {
+        energy[0] = energy[1] = 0.0;
+        return SDT_OK;
+    }
+    int rc = cuda_check(cudaMemsetAsync(p->err_d, 0, sizeof(int), st), "plan finish");
+    if (!rc) rc = plan_sums(p, st);
+    if (!rc) rc = plan_read(p, st, energy, nullptr, "plan finish");
+    return rc;
+}
+
+void plan_release(sdt_plan *p) { plan_free(p); }
 }  // namespace sdt
 
 using namespace sdt;

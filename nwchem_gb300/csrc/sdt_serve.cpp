@@ -2,21 +2,32 @@
 // reference counterpart: NWChem evaluates one (T) problem per run).
 //
 // Clients submit jobs (a tiling and its T1/T2/V2 files) at any time.  Jobs
-// wait in one FIFO queue; a job is admitted when one of the server's slots
-// is free and its device bytes fit in the HBM budget minus the bytes of the
-// jobs already admitted (a job larger than the whole budget is rejected).
-// Each slot is a worker thread; an admitted job runs on its own CUDA stream:
-// device tables, H2D copy and ingest of its files, the mixed form's operand
-// encoding, the persistent kernel over all its tuples (work-unit shape chosen
-// from the job's contraction length) and the energy sums, and its memory is
-// returned.  A job with an FP64 check keeps its device memory (and its
-// admitted bytes) after its energies are delivered; the check runs when no
-// admissible job is waiting, so checks do not hold back the stream.
-// Jobs admitted together overlap on the device -- one job's copies and
-// encoding with another's contraction kernel, and their kernels at launch
-// boundaries (or throughout, with max_ctas capping each job's CTAs).  A
+// wait in one FIFO queue; a job is admitted when fewer than `slots` jobs are
+// in flight and its device bytes fit in the HBM budget minus the bytes of
+// the jobs already admitted (a job larger than the whole budget is
+// rejected).  `slots` worker threads admit and load jobs: device tables, H2D
+// copy and ingest of the files, the mixed form's operand encoding and the
+// job's work index, each job on its own CUDA stream.
+//
+// Continuous batching (the default, for jobs of the server's mixed form):
+// a loaded job's sub-box items are appended to one shared device queue that
+// a resident persistent kernel drains -- the job's parameters go into a
+// device job table and the queue's tail grows by its item count, while the
+// kernel runs.  The kernel holds all SMs but `reserve` of them, which stay
+// free for the loading, encoding and final sums of other jobs and for FP64
+// checks, so jobs arriving while others compute are loaded and enter the
+// same queue.  The kernel counts each job's finished items and the last one
+// sets a host-visible flag; a monitor thread then runs the job's per-tuple
+// and total sums, delivers its energies and returns its memory.  The kernel
+// leaves after a quiet period with nothing to take; the monitor launches it
+// again when work is appended.  Other precisions run one launch per job.
+//
+// A job with an FP64 check keeps its device memory (and its admitted bytes)
+// after its energies are delivered; the check runs when no admissible job is
+// waiting, on `check_ctas` SMs, so checks do not hold back the stream.  A
 // job's result depends only on its inputs, never on what ran beside it.
 #include "sdt_internal.h"
+#include "sdt_job.h"
 
 #include <cuda_runtime.h>
 
@@ -122,7 +133,35 @@ struct sdt_server {
         std::string msg;
         sdt_job *held = nullptr;  // kept on the device for the deferred FP64 check
         std::vector<int64_t> kl;
+        // shared-queue jobs: device data and plan while queued, queue slot,
+        // launch numbers that took the first and finished the last item
+        sdt_job *dj = nullptr;
+        sdt_plan *plan = nullptr;
+        int slot = -1, first_gen = 0, last_gen = 0;
     };
+    // The shared item queue (continuous batching), set up at its first use.
+    struct Queue {
+        int precision = SDT_PREC_MIXED_FP16, type = TM_F16, shape = 2, reserve = 16, max_jobs = 4096;
+        double idle_s = 0.2;
+        bool ready = false;
+        size_t entry = 0;
+        void *table_d = nullptr;
+        long long *base_d = nullptr;
+        unsigned long long *head_d = nullptr, *tail_d = nullptr, *done_d = nullptr;
+        int *close_d = nullptr, *err_d = nullptr;
+        int *gen_h = nullptr, *gen_dp = nullptr;  // host-mapped [2][max_jobs]: first / last launch per slot
+        uint8_t *stage_h = nullptr;               // pinned: table entries, bases, tails, read-back
+        cudaStream_t kst = nullptr, pst = nullptr;
+        cudaEvent_t kev = nullptr;
+        bool running = false;
+        int gen = 0, next_slot = 0, grid = 0;
+        unsigned long long tail = 0;
+        int64_t launches = 0, jobs = 0, in_flight = 0, max_in_flight = 0;
+        std::vector<Job *> by_slot;
+        std::mutex mu;
+    } q;
+    std::thread monitor;
+    bool use_queue = true, mon_stop = false;
     int64_t budget = 0;
     int slots = 1, max_ctas = 0;
     int sms = 0, check_ctas = 0, checks_running = 0;
@@ -208,6 +247,300 @@ void run_one(sdt_server *s, sdt_server::Job *job) {
     sdt_job_destroy(j);
 }
 
+// ---------------------------------------------------------------------------
+// The shared item queue.
+
+constexpr long long kUnusedBase = 0x7fffffffffffffffll;
+
+// Device and pinned buffers of the queue and its two streams (q.mu held).
+int queue_setup(sdt_server *s) {
+    auto &Q = s->q;
+    if (Q.ready) return SDT_OK;
+    Q.entry = mixed_job_entry_bytes();
+    Q.by_slot.assign(Q.max_jobs, nullptr);
+    Q.grid = std::max(1, s->sms - Q.reserve);
+    int rc = mixed_queue_prepare(Q.type, Q.shape);
+    auto dev = [&](void **p, size_t bytes) {
+        if (!rc) rc = cuda_check(cudaMalloc(p, bytes), "sdt_server: queue buffers");
+    };
+    dev(&Q.table_d, Q.entry * Q.max_jobs);
+    dev((void **)&Q.base_d, sizeof(long long) * Q.max_jobs);
+    dev((void **)&Q.done_d, sizeof(unsigned long long) * Q.max_jobs);
+    dev((void **)&Q.head_d, 2 * sizeof(unsigned long long));
+    dev((void **)&Q.close_d, 2 * sizeof(int));
+    if (Q.head_d) Q.tail_d = Q.head_d + 1;
+    if (Q.close_d) Q.err_d = Q.close_d + 1;
+    if (!rc) rc = cuda_check(cudaHostAlloc((void **)&Q.gen_h, 2 * sizeof(int) * Q.max_jobs, cudaHostAllocMapped),
+                             "sdt_server: queue flags");
+    if (!rc) rc = cuda_check(cudaHostGetDevicePointer((void **)&Q.gen_dp, Q.gen_h, 0), "sdt_server: queue flags");
+    if (!rc) rc = cuda_check(cudaHostAlloc((void **)&Q.stage_h, (Q.entry + 16) * Q.max_jobs + 64, cudaHostAllocDefault),
+                             "sdt_server: queue staging");
+    if (!rc) rc = cuda_check(cudaStreamCreateWithFlags(&Q.kst, cudaStreamNonBlocking), "sdt_server: queue stream");
+    if (!rc) rc = cuda_check(cudaStreamCreateWithFlags(&Q.pst, cudaStreamNonBlocking), "sdt_server: queue stream");
+    if (!rc) rc = cuda_check(cudaEventCreateWithFlags(&Q.kev, cudaEventDisableTiming), "sdt_server: queue event");
+    if (rc) return rc;
+    Q.ready = true;
+    Q.next_slot = Q.max_jobs;  // the first publish resets the queue
+    return SDT_OK;
+}
+
+long long *stage_base(sdt_server::Queue &Q) { return (long long *)(Q.stage_h + Q.entry * Q.max_jobs); }
+unsigned long long *stage_tail(sdt_server::Queue &Q) {
+    return (unsigned long long *)(Q.stage_h + (Q.entry + 8) * Q.max_jobs);
+}
+int *stage_word(sdt_server::Queue &Q) { return (int *)(Q.stage_h + (Q.entry + 16) * Q.max_jobs); }
+
+// Empties the queue for a new round of slots (no kernel running, no job in
+// flight; q.mu held).
+int queue_reset(sdt_server *s) {
+    auto &Q = s->q;
+    int rc = cuda_check(cudaMemsetAsync(Q.base_d, 0x7f, sizeof(long long) * Q.max_jobs, Q.pst), "sdt_server: queue");
+    if (!rc) rc = cuda_check(cudaMemsetAsync(Q.done_d, 0, sizeof(unsigned long long) * Q.max_jobs, Q.pst), "sdt_server");
+    if (!rc) rc = cuda_check(cudaMemsetAsync(Q.head_d, 0, 2 * sizeof(unsigned long long), Q.pst), "sdt_server");
+    if (!rc) rc = cuda_check(cudaMemsetAsync(Q.close_d, 0, 2 * sizeof(int), Q.pst), "sdt_server");
+    if (!rc) rc = cuda_check(cudaStreamSynchronize(Q.pst), "sdt_server: queue reset");
+    std::memset(Q.gen_h, 0, 2 * sizeof(int) * Q.max_jobs);
+    std::fill(Q.by_slot.begin(), Q.by_slot.end(), nullptr);
+    Q.next_slot = 0;
+    Q.tail = 0;
+    return rc;
+}
+
+// Notes a finished kernel (q.mu held): returns its error code, 0 if none.
+int queue_reap(sdt_server *s) {
+    auto &Q = s->q;
+    if (!Q.running) return SDT_OK;
+    const cudaError_t e = cudaEventQuery(Q.kev);
+    if (e == cudaErrorNotReady) return SDT_OK;
+    Q.running = false;
+    int rc = cuda_check(e, "sdt_server: queue kernel");
+    int *w = stage_word(Q);
+    if (!rc) rc = cuda_check(cudaMemcpyAsync(w, Q.err_d, sizeof(int), cudaMemcpyDeviceToHost, Q.pst), "sdt_server");
+    if (!rc) rc = cuda_check(cudaStreamSynchronize(Q.pst), "sdt_server");
+    if (!rc && *w)
+        rc = fail(SDT_ERR_TIMEOUT, "sdt_server: a bounded wait in the queue kernel ran out (code " +
+                                       std::to_string(*w) + ")");
+    return rc;
+}
+
+// Launches the resident kernel when it is not running and queue positions
+// are left to take (q.mu held).
+int queue_ensure(sdt_server *s) {
+    auto &Q = s->q;
+    int rc = queue_reap(s);
+    if (rc || Q.running || Q.in_flight == 0) return rc;
+    unsigned long long head = 0;
+    rc = cuda_check(cudaMemcpyAsync(stage_word(Q) + 2, Q.head_d, sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+                                    Q.pst), "sdt_server");
+    if (!rc) rc = cuda_check(cudaStreamSynchronize(Q.pst), "sdt_server");
+    if (rc) return rc;
+    std::memcpy(&head, stage_word(Q) + 2, sizeof(head));
+    if (head >= Q.tail) return SDT_OK;  // every published item is taken (and, with no kernel, finished)
+    QueueArgs a;
+    a.table = Q.table_d;
+    a.base = Q.base_d;
+    a.head = Q.head_d;
+    a.tail = Q.tail_d;
+    a.done = Q.done_d;
+    a.first_gen = Q.gen_dp;
+    a.last_gen = Q.gen_dp + Q.max_jobs;
+    a.close = Q.close_d;
+    a.err = Q.err_d;
+    a.idle_ns = (unsigned long long)(Q.idle_s * 1e9);
+    a.max_jobs = Q.max_jobs;
+    a.gen = ++Q.gen;
+    rc = cuda_check(cudaMemsetAsync(Q.close_d, 0, 2 * sizeof(int), Q.pst), "sdt_server");
+    cudaEvent_t ev = nullptr;
+    if (!rc) rc = cuda_check(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming), "sdt_server");
+    if (!rc) rc = cuda_check(cudaEventRecord(ev, Q.pst), "sdt_server");
+    if (!rc) rc = cuda_check(cudaStreamWaitEvent(Q.kst, ev, 0), "sdt_server");
+    if (ev) cudaEventDestroy(ev);
+    if (!rc) rc = mixed_queue_launch(Q.type, Q.shape, a, Q.grid, Q.kst);
+    if (!rc) rc = cuda_check(cudaEventRecord(Q.kev, Q.kst), "sdt_server");
+    if (!rc) {
+        Q.running = true;
+        ++Q.launches;
+    }
+    return rc;
+}
+
+constexpr int kRetry = -1;
+
+// Appends a loaded job's items to the queue (q.mu held).  kRetry: the slot
+// table is used up and in use; call again once the queue has emptied.
+int queue_publish(sdt_server *s, sdt_server::Job *job) {
+    auto &Q = s->q;
+    int rc = queue_setup(s);
+    if (rc) return rc;
+    if (Q.next_slot >= Q.max_jobs) {
+        // a new round of slots: only once the queue is idle and empty
+        if (Q.in_flight > 0) return kRetry;
+        rc = queue_reap(s);
+        if (rc) return rc;
+        if (Q.running) return kRetry;
+        rc = queue_reset(s);
+        if (rc) return rc;
+    }
+    const int slot = Q.next_slot++;
+    uint8_t *ent = Q.stage_h + Q.entry * slot;
+    int64_t items = 0;
+    rc = plan_queue_entry(job->plan, ent, &items);
+    if (rc) return rc;
+    stage_base(Q)[slot] = (long long)Q.tail;
+    Q.tail += (unsigned long long)items;
+    stage_tail(Q)[slot] = Q.tail;
+    if (!rc) rc = cuda_check(cudaMemcpyAsync((uint8_t *)Q.table_d + Q.entry * slot, ent, Q.entry,
+                                             cudaMemcpyHostToDevice, Q.pst), "sdt_server: publish");
+    if (!rc) rc = cuda_check(cudaMemcpyAsync(Q.base_d + slot, stage_base(Q) + slot, sizeof(long long),
+                                             cudaMemcpyHostToDevice, Q.pst), "sdt_server: publish");
+    // the tail last: the kernel reads an entry only below the tail
+    if (!rc) rc = cuda_check(cudaMemcpyAsync(Q.tail_d, stage_tail(Q) + slot, sizeof(unsigned long long),
+                                             cudaMemcpyHostToDevice, Q.pst), "sdt_server: publish");
+    if (rc) return rc;
+    job->slot = slot;
+    Q.by_slot[slot] = job;
+    ++Q.in_flight;
+    ++Q.jobs;
+    Q.max_in_flight = std::max(Q.max_in_flight, Q.in_flight);
+    return queue_ensure(s);
+}
+
+std::string take_error() {
+    char buf[512] = {0};
+    sdt_last_error(buf, sizeof(buf));
+    return buf;
+}
+
+// Loads a job and appends its items to the shared queue.  true: the job is
+// in the queue (the monitor completes it); false: it finished here (an
+// error, or no tuples).
+bool run_queued(sdt_server *s, sdt_server::Job *job) {
+    cudaSetDevice(s->device);
+    sdt_job *j = nullptr;
+    int rc = sdt_job_create(&job->t, &j);
+    if (!rc) rc = sdt_job_load(j, &job->f1, &job->f2, &job->fv, nullptr);
+    int64_t n = 0;
+    if (!rc) {
+        n = sdt_tasks_count(&job->t);
+        job->kl.resize(7 * std::max<int64_t>(n, 1));
+        rc = n < 0 ? SDT_ERR_ARG : sdt_tasks_list(&job->t, n, job->kl.data());
+        if (!rc) job->kl.resize(7 * n);
+    }
+    if (!rc && n > 0) {
+        std::vector<int32_t> shapes(n, s->q.shape);
+        rc = plan_make(j, job->kl.data(), n, s->q.precision, shapes.data(), &job->plan);
+    }
+    job->t_loaded = s->now();
+    if (!rc && n > 0) {
+        job->dj = j;
+        while (true) {
+            {
+                std::lock_guard<std::mutex> lk(s->q.mu);
+                rc = queue_publish(s, job);
+            }
+            if (rc != kRetry) break;
+            std::this_thread::sleep_for(std::chrono::milliseconds(1));
+        }
+        if (!rc) return true;
+        job->dj = nullptr;
+    }
+    if (rc) {
+        job->err = rc;
+        job->msg = take_error();
+    }
+    job->t_ran = s->now();
+    if (job->plan) plan_release(job->plan);
+    job->plan = nullptr;
+    if (!rc && job->check) {
+        job->held = j;
+        return false;
+    }
+    sdt_job_destroy(j);
+    return false;
+}
+
+// A queued job whose items are all finished: its sums and energies, then
+// its memory is returned (or kept for its FP64 check).
+void queue_finish(sdt_server *s, sdt_server::Job *job, int rc_in) {
+    int rc = rc_in;
+    if (!rc) rc = plan_finish(job->plan, (cudaStream_t)sdt_job_stream(job->dj), job->e);
+    if (rc) {
+        job->err = rc;
+        job->msg = rc_in ? "sdt_server: the queue kernel failed: " + take_error() : take_error();
+    }
+    job->t_ran = s->now();
+    plan_release(job->plan);
+    job->plan = nullptr;
+    if (!rc && job->check) {
+        job->held = job->dj;
+    } else {
+        sdt_job_destroy(job->dj);
+    }
+    job->dj = nullptr;
+    std::lock_guard<std::mutex> lk(s->mu);
+    if (job->held) {
+        s->adm.free_slot();
+        job->state = 3;
+        s->checks.push_back(job);
+    } else {
+        s->adm.release(job->bytes);
+        job->t_end = s->now();
+        job->state = job->err ? -1 : 2;
+    }
+    s->cv.notify_all();
+}
+
+// Completes queued jobs as their last items finish and keeps the resident
+// kernel running while queue positions are left to take.
+void monitor(sdt_server *s) {
+    cudaSetDevice(s->device);
+    auto &Q = s->q;
+    while (true) {
+        std::vector<sdt_server::Job *> done;
+        int rc = SDT_OK;
+        bool stop = false;
+        {
+            std::lock_guard<std::mutex> lk(Q.mu);
+            if (Q.ready) {
+                const volatile int *last = Q.gen_h + Q.max_jobs;
+                for (int slot = 0; slot < Q.next_slot && slot < Q.max_jobs; ++slot) {
+                    sdt_server::Job *job = Q.by_slot[slot];
+                    if (!job || last[slot] == 0) continue;
+                    job->first_gen = ((const volatile int *)Q.gen_h)[slot];
+                    job->last_gen = last[slot];
+                    Q.by_slot[slot] = nullptr;
+                    --Q.in_flight;
+                    done.push_back(job);
+                }
+                rc = queue_ensure(s);
+                if (rc) {  // the kernel failed: every job still in the queue fails with it
+                    for (int slot = 0; slot < Q.max_jobs; ++slot)
+                        if (Q.by_slot[slot]) {
+                            done.push_back(Q.by_slot[slot]);
+                            Q.by_slot[slot] = nullptr;
+                        }
+                    Q.in_flight = 0;
+                    Q.next_slot = Q.max_jobs;  // the next publish starts a fresh queue
+                }
+            }
+            stop = s->mon_stop && Q.in_flight == 0;
+        }
+        for (auto *job : done) queue_finish(s, job, (rc && job->last_gen == 0) ? rc : SDT_OK);
+        if (stop) break;
+        if (done.empty()) std::this_thread::sleep_for(std::chrono::microseconds(100));
+    }
+    // close the resident kernel and wait for it (its wait for work is bounded)
+    std::lock_guard<std::mutex> lk(Q.mu);
+    if (Q.ready && Q.running) {
+        int one = 1;
+        std::memcpy(stage_word(Q), &one, sizeof(int));
+        cudaMemcpyAsync(Q.close_d, stage_word(Q), sizeof(int), cudaMemcpyHostToDevice, Q.pst);
+        cudaStreamSynchronize(Q.pst);
+        cudaEventSynchronize(Q.kev);
+        Q.running = false;
+    }
+}
+
 // The deferred FP64 check of a held job, then its device memory is returned.
 void run_check(sdt_server *s, sdt_server::Job *job) {
     cudaSetDevice(s->device);
@@ -266,9 +599,16 @@ void worker(sdt_server *s) {
         s->adm.admit(job->bytes);
         job->state = 1;
         job->t_start = s->now();
+        const bool queued = s->use_queue && job->precision == s->q.precision;
         lk.unlock();
-        run_one(s, job);
+        bool in_queue = false;
+        if (queued) in_queue = run_queued(s, job);
+        else run_one(s, job);
         lk.lock();
+        if (in_queue) {  // the monitor completes it
+            s->cv.notify_all();
+            continue;
+        }
         if (job->held) {  // energies delivered; memory kept for the check
             s->adm.free_slot();
             job->state = 3;
@@ -303,9 +643,56 @@ extern "C" int sdt_server_create(int64_t budget_bytes, int slots, int max_ctas, 
         cudaGetLastError();
         s->sms = 0;
     }
-    s->check_ctas = s->sms / 4;
+    s->check_ctas = std::max(1, s->q.reserve / 2);  // checks leave half the kernel-free SMs to job loads
     for (int k = 0; k < slots; ++k) s->workers.emplace_back(worker, s);
+    s->monitor = std::thread(monitor, s);
     *out = s;
+    return SDT_OK;
+}
+
+// The shared queue's form (precision; 0 turns the queue off: every job gets
+// its own launches), work-unit shape (1 or 2), the SMs kept free of the
+// resident kernel, and how long the kernel waits for work before it leaves.
+// Before the first submit.
+extern "C" int sdt_server_set_queue(sdt_server *s, int precision, int shape, int reserve_sms, double idle_s) {
+    if (!s || precision < SDT_PREC_FP64 || precision > SDT_PREC_MIXED_FP16 || (shape != 1 && shape != 2) ||
+        reserve_sms < 1 || !(idle_s > 0.0) || idle_s > 1.0)
+        return fail(SDT_ERR_ARG, "sdt_server_set_queue: bad argument");
+    std::lock_guard<std::mutex> lk(s->mu);
+    std::lock_guard<std::mutex> lq(s->q.mu);
+    if (!s->jobs.empty() || s->q.ready) return fail(SDT_ERR_STATE, "sdt_server_set_queue: jobs were submitted");
+    if (s->sms > 0 && reserve_sms >= s->sms) return fail(SDT_ERR_ARG, "sdt_server_set_queue: no SM left for the queue");
+    s->use_queue = precision != SDT_PREC_FP64;
+    s->q.precision = precision;
+    s->q.type = precision == SDT_PREC_MIXED_TF32 ? TM_F32 : precision == SDT_PREC_MIXED_BF16 ? TM_BF16 : TM_F16;
+    s->q.shape = shape;
+    s->q.reserve = reserve_sms;
+    s->q.idle_s = idle_s;
+    s->check_ctas = s->use_queue ? std::max(1, reserve_sms / 2) : s->sms / 4;
+    return SDT_OK;
+}
+
+// stats[0] resident-kernel launches, [1] jobs that went through the queue,
+// [2] most jobs in the queue at once, [3] jobs in it now.
+extern "C" int sdt_server_queue_stats(sdt_server *s, int64_t *stats) {
+    if (!s || !stats) return fail(SDT_ERR_ARG, "sdt_server_queue_stats: null argument");
+    std::lock_guard<std::mutex> lk(s->q.mu);
+    stats[0] = s->q.launches;
+    stats[1] = s->q.jobs;
+    stats[2] = s->q.max_in_flight;
+    stats[3] = s->q.in_flight;
+    return SDT_OK;
+}
+
+// The resident-kernel launches (numbered from 1) that took a queued job's
+// first item and finished its last one; 0 for a job that did not go through
+// the queue (or has not finished).
+extern "C" int sdt_server_job_launches(sdt_server *s, int64_t ticket, int *first, int *last) {
+    if (!s || !first || !last) return fail(SDT_ERR_ARG, "sdt_server_job_launches: null argument");
+    std::lock_guard<std::mutex> lk(s->mu);
+    if (ticket < 0 || ticket >= (int64_t)s->jobs.size()) return fail(SDT_ERR_ARG, "sdt_server_job_launches: bad ticket");
+    *first = s->jobs[ticket]->first_gen;
+    *last = s->jobs[ticket]->last_gen;
     return SDT_OK;
 }
 
@@ -428,11 +815,29 @@ extern "C" int sdt_server_destroy(sdt_server *s) {
         s->cv.notify_all();
     }
     for (auto &w : s->workers) w.join();
+    {
+        std::lock_guard<std::mutex> lq(s->q.mu);
+        s->mon_stop = true;  // the monitor finishes the queued jobs, then closes the kernel
+    }
+    if (s->monitor.joinable()) s->monitor.join();
     for (auto &job : s->jobs)
         if (job->held) {
             sdt_job_destroy(job->held);
             job->held = nullptr;
         }
+    auto &Q = s->q;
+    if (Q.ready) {
+        cudaFree(Q.table_d);
+        cudaFree(Q.base_d);
+        cudaFree(Q.done_d);
+        cudaFree(Q.head_d);
+        cudaFree(Q.close_d);
+        cudaFreeHost(Q.gen_h);
+        cudaFreeHost(Q.stage_h);
+        cudaStreamDestroy(Q.kst);
+        cudaStreamDestroy(Q.pst);
+        cudaEventDestroy(Q.kev);
+    }
     delete s;
     return SDT_OK;
 }

@@ -119,14 +119,22 @@ __device__ __forceinline__ int xaddr(int a, int b, int c, int i, int j, int k) {
            (((i + k) & 3) << 2) | ((j + k) & 3);
 }
 
-// What the energy chunks of an item need after its last drain.
+// What the energy chunks of an item need after its last drain: the sub-box
+// and the job data it reads and writes (several jobs may share a launch).
 struct EDesc {
     int g[6];       // global orbital index of the sub-box origin, per dimension
     int nv[6];      // valid extent of the sub-box, per dimension
     int gp[6];      // holes (3..5): padded hole index of the origin (FP32 s1 copies)
+    int op;         // padded hole count of the job's FP32 copies
     double factor;  // the tuple's multiplicity factor
-    long long item;
+    long long item; // the item's index within its job
+    const float *T1f, *Uf;      // the job's FP32 copies of T1 and the vvoo block
+    const double *eo, *ev;      // its occupied and virtual orbital energies
+    double *part;               // its per-item energy pairs
+    double inv_s, inv_s2;       // its operand scaling
+    long long nvir;
 };
+static_assert(sizeof(EDesc) <= 192, "EDesc fits its shared-memory slot");
 
 // Split operands live in HBM "block-major": one block per (row boxes, K chunk)
 // holds a whole stage tile -- 128 rows (A) or 256 rows (B) of 32 bytes, in the
@@ -140,7 +148,7 @@ struct EDesc {
 //   Vd2 (d2 B)  per tile pair (B<=C): [lb0][lb1][H][kc_v], lb local boxes
 enum { L_WD1 = 0, L_T2B, L_T2A, L_VD2, L_N };
 
-struct SplitParams {
+struct alignas(16) SplitParams {
     const uint8_t *blk[2 * L_N];  // [2*layout + (0 hi, 1 lo)]
     const int32_t *tile_box;      // [ntiles]: global box id of the tile's first box (its space)
     const int64_t *pair_blk;      // [nvab*nvab]: first Vd2 block of tile pair (B<=C), -1 none
@@ -159,6 +167,76 @@ struct SplitParams {
     unsigned long long *queue;    // item counter, zero at launch
     int32_t all_k;                // every K tile allowed for every term (one spin, no irreps)
 };
+
+static_assert(sizeof(SplitParams) % 16 == 0, "job parameters copy in 16-byte pieces");
+
+// The shared item queue of the serving path: several jobs' items, drawn by
+// one resident launch.  The host appends a job by writing its parameters to
+// table[slot] and its first queue position to base[slot], then raising
+// tail by the job's item count (queue positions base .. base + items - 1).
+// CTAs take positions one at a time (never past tail), leave when nothing
+// is left to take for idle_ns or when close is set, and count each job's
+// finished items; the CTA that finishes a job's last item stores the launch
+// number in last_gen[slot] (host-mapped memory), which is how the host
+// learns that the job's per-item energies are complete.
+struct QueueCtl {
+    const SplitParams *table;        // [max_jobs]
+    const long long *base;           // [max_jobs]; LLONG_MAX for slots not yet used
+    unsigned long long *head;        // next position to take
+    const unsigned long long *tail;  // positions published
+    unsigned long long *done;        // [max_jobs] finished items per job
+    int *first_gen, *last_gen;       // [max_jobs] host-mapped: launch that took the job's first / finished its last item
+    const int *close;
+    int *err;
+    unsigned long long idle_ns;
+    int max_jobs, gen;
+};
+constexpr int kSlotShift = 40;       // queue-mode ring entries: slot << 40 | item within the job
+constexpr long long kItemMask = (1ll << kSlotShift) - 1;
+
+__device__ __forceinline__ unsigned long long ld_volatile(const unsigned long long *p) {
+    return *(const volatile unsigned long long *)p;
+}
+
+// Takes the next queue position (-1: nothing to take for idle_ns, or close).
+__device__ __forceinline__ long long claim_position(const QueueCtl &q, volatile int *abort) {
+    const uint64_t t0 = tc::global_ns();
+    unsigned pause = 64;
+    while (true) {
+        const unsigned long long h = ld_volatile(q.head), t = ld_volatile(q.tail);
+        if (h < t) {
+            if (atomicCAS(q.head, h, h + 1) == h) {
+                __threadfence();  // the job's table entry was written before tail grew
+                return (long long)h;
+            }
+            continue;
+        }
+        if (*abort || *(const volatile int *)q.close) return -1;
+        if (tc::global_ns() - t0 > q.idle_ns) return -1;
+        __nanosleep(pause);
+        if (pause < 8192) pause *= 2;
+    }
+}
+
+// Slot of queue position pos: the last slot whose base is <= pos (unused
+// slots hold LLONG_MAX).  Read through L2 only: the host rewrites entries
+// while the launch runs.
+__device__ __forceinline__ int find_slot(const QueueCtl &q, long long pos) {
+    int lo = 0, hi = q.max_jobs - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (__ldcg(q.base + mid) <= pos) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+__device__ __forceinline__ void load_job(const QueueCtl &q, int slot, SplitParams &out) {
+    const uint4 *src = reinterpret_cast<const uint4 *>(q.table + slot);
+    uint4 *dst = reinterpret_cast<uint4 *>(&out);
+#pragma unroll
+    for (int k = 0; k < (int)(sizeof(SplitParams) / 16); ++k) dst[k] = __ldcg(src + k);
+}
 
 struct ItemBox {
     int tile[6], start[6], ext[6], boff[6], lbox[6];  // lbox: local box, clamped into the tile
@@ -290,25 +368,46 @@ __device__ __forceinline__ void bulk_load(void *dst, const void *src, uint32_t b
 }
 
 // ---------------------------------------------------------------------------
-// Operand producer (one thread): per stage, the A and B blocks (hi, lo) of
-// the term's K chunk, four contiguous bulk copies.
-template <int TYPE>
-__device__ __forceinline__ void run_producer(const SplitParams &p, uint8_t *stages, uint64_t *full,
-                                             uint64_t *empty, volatile int *abort, const UnitRing &ring) {
+// Operand producer (one thread): takes the next item (from the launch's own
+// counter, or in queue mode the next queue position and its job's table
+// entry), publishes it to the other roles, and per stage issues the A and B
+// blocks (hi, lo) of the term's K chunk, four contiguous bulk copies.
+template <int TYPE, int QUEUE>
+__device__ __forceinline__ void run_producer(const SplitParams &gp, const QueueCtl &q, uint8_t *stages,
+                                             uint64_t *full, uint64_t *empty, volatile int *abort,
+                                             const UnitRing &ring) {
     constexpr int KE = TYPE == TM_F32 ? 8 : 16;  // K values per 32-byte row
-    const int64_t NOB = p.nob, NVB = p.nvb;
+    SplitParams lp;                              // queue mode: the current item's job
     uint32_t g = 0;
     bool stop = false;
     for (int n = 0; !stop; ++n) {
-        const unsigned long long u = atomicAdd(p.queue, 1ull);
-        const int64_t si = u < (unsigned long long)p.n_items ? (int64_t)u : -1;
-        if (!ring_publish(ring, n, si, abort)) {
+        int64_t unit, item = 0;
+        if (QUEUE) {
+            const long long pos = claim_position(q, abort);
+            unit = -1;
+            if (pos >= 0) {
+                const int slot = find_slot(q, pos);
+                item = pos - __ldcg(q.base + slot);
+                unit = ((int64_t)slot << kSlotShift) | item;
+                load_job(q, slot, lp);
+                if (item == 0) {
+                    *(volatile int *)(q.first_gen + slot) = q.gen;
+                    __threadfence_system();
+                }
+            }
+        } else {
+            const unsigned long long u = atomicAdd(gp.queue, 1ull);
+            unit = item = u < (unsigned long long)gp.n_items ? (int64_t)u : -1;
+        }
+        if (!ring_publish(ring, n, unit, abort)) {
             stop = true;
             break;
         }
-        if (si < 0) break;
+        if (unit < 0) break;
+        const SplitParams &p = QUEUE ? lp : gp;
+        const int64_t NOB = p.nob, NVB = p.nvb;
         ItemBox bx;
-        decode_item(p, si, bx);
+        decode_item(p, item, bx);
         int gb[6];  // global box ids
 #pragma unroll
         for (int d = 0; d < 6; ++d) gb[d] = __ldg(p.tile_box + bx.tile[d] - 1) + bx.lbox[d];
@@ -346,7 +445,7 @@ __device__ __forceinline__ void run_producer(const SplitParams &p, uint8_t *stag
     }
     if (stop) {
         *abort = 1;
-        atomicCAS(p.err, 0, 1);
+        atomicCAS(QUEUE ? q.err : gp.err, 0, 1);
         // copies already issued must land before the CTA exits
         volatile int never = 0;
         for (uint32_t x = g >= SX_NS ? g - SX_NS : 0; x < g; ++x)
@@ -356,19 +455,22 @@ __device__ __forceinline__ void run_producer(const SplitParams &p, uint8_t *stag
 
 // ---------------------------------------------------------------------------
 // MMA issuer (one thread).
-template <int TYPE, int NB>
-__device__ __forceinline__ void run_mma(const SplitParams &p, uint8_t *stages, uint64_t *full, uint64_t *empty,
-                                        uint64_t *tfull, uint64_t *tempty, uint64_t *drain, uint32_t tmem,
-                                        volatile int *abort, const UnitRing &ring) {
+template <int TYPE, int NB, int QUEUE>
+__device__ __forceinline__ void run_mma(const SplitParams &gp, const QueueCtl &q, uint8_t *stages, uint64_t *full,
+                                        uint64_t *empty, uint64_t *tfull, uint64_t *tempty, uint64_t *drain,
+                                        uint32_t tmem, volatile int *abort, const UnitRing &ring) {
     constexpr int KE = TYPE == TM_F32 ? 8 : 16;
+    SplitParams lp;
     uint32_t g = 0, sg = 0;  // stage and segment counters
     bool stop = false;
     for (int n = 0; !stop; ++n) {
-        const int64_t si = ring_take(ring, n, abort);
-        if (si == -2) stop = true;
-        if (si < 0) break;
+        const int64_t unit = ring_take(ring, n, abort);
+        if (unit == -2) stop = true;
+        if (unit < 0) break;
+        if (QUEUE) load_job(q, (int)(unit >> kSlotShift), lp);
+        const SplitParams &p = QUEUE ? lp : gp;
         ItemBox bx;
-        decode_item(p, si, bx);
+        decode_item(p, QUEUE ? (unit & kItemMask) : unit, bx);
         for (int t = 0; t < 9 && !stop; ++t) {
             const int nk = term_chunk_count<KE>(p, bx, t);
             int kseg;
@@ -403,7 +505,7 @@ __device__ __forceinline__ void run_mma(const SplitParams &p, uint8_t *stages, u
     }
     if (stop) {
         *abort = 1;
-        atomicCAS(p.err, 0, 2);
+        atomicCAS(QUEUE ? q.err : gp.err, 0, 2);
     }
     // every issued MMA completes before TMEM is released
     tc::mma_commit(drain);
@@ -505,36 +607,36 @@ __device__ __forceinline__ float el(const float4 &x, int k) { return k == 0 ? x.
 // multiple of 4 holes, so the 4 k values of a sub-box are one aligned float4.
 // R[OFF + 4*c + k] holds local (a = 4*half + A, b, c, i, j, k).
 template <int A, int OFF, int N>
-__device__ __forceinline__ void energy_chunk(const float (&R)[N], const EDesc &d, const SplitParams &p, int half,
-                                             int b, int i, int j, double &e1, double &est) {
+__device__ __forceinline__ void energy_chunk(const float (&R)[N], const EDesc &d, int half, int b, int i, int j,
+                                             double &e1, double &est) {
     const int a = 4 * half + A;
     if (a >= d.nv[0] || b >= d.nv[1] || i >= d.nv[3] || j >= d.nv[4]) return;
-    const int op = p.op;
-    const int64_t v = p.nvir, oo = (int64_t)op * op;
+    const int op = d.op;
+    const int64_t v = d.nvir, oo = (int64_t)op * op;
     const int ga = d.g[0] + a, gb = d.g[1] + b, gi = d.g[3] + i, gj = d.g[4] + j;
     const int pi = d.gp[3] + i, pj = d.gp[4] + j, pk0 = d.gp[5];  // padded holes
     const int nc = d.nv[2], nk = d.nv[5], gc0 = d.g[2], gk0 = d.g[5];
-    const double *__restrict__ eo = p.evl;
-    const double *__restrict__ ev = p.evl + p.nocc;
+    const double *__restrict__ eo = d.eo;
+    const double *__restrict__ ev = d.ev;
     const double eij = __ldg(eo + gi) + __ldg(eo + gj);
     const double eab = __ldg(ev + ga) + __ldg(ev + gb);
     double P[4];  // e_i + e_j + e_k
 #pragma unroll
     for (int k = 0; k < 4; ++k) P[k] = k < nk ? eij + __ldg(eo + gk0 + k) : 0.0;
-    const float *__restrict__ t1a = p.T1f + (int64_t)ga * op;
-    const float *__restrict__ t1b = p.T1f + (int64_t)gb * op;
+    const float *__restrict__ t1a = d.T1f + (int64_t)ga * op;
+    const float *__restrict__ t1b = d.T1f + (int64_t)gb * op;
     const float t1ai = __ldg(t1a + pi), t1aj = __ldg(t1a + pj), t1bi = __ldg(t1b + pi), t1bj = __ldg(t1b + pj);
     const float4 t1ak = ld4(t1a + pk0), t1bk = ld4(t1b + pk0);
-    const float *__restrict__ uab = p.Uf + ((int64_t)ga * v + gb) * oo;
+    const float *__restrict__ uab = d.Uf + ((int64_t)ga * v + gb) * oo;
     const float uabij = __ldg(uab + pi * op + pj);
     const float4 uabj = ld4(uab + pj * op + pk0), uabi = ld4(uab + pi * op + pk0);
 #pragma unroll
     for (int c = 0; c < 8; ++c) {
         if (c < nc) {
             const int gc = gc0 + c;
-            const float *__restrict__ t1c = p.T1f + (int64_t)gc * op;
-            const float *__restrict__ ubc = p.Uf + ((int64_t)gb * v + gc) * oo;
-            const float *__restrict__ uac = p.Uf + ((int64_t)ga * v + gc) * oo;
+            const float *__restrict__ t1c = d.T1f + (int64_t)gc * op;
+            const float *__restrict__ ubc = d.Uf + ((int64_t)gb * v + gc) * oo;
+            const float *__restrict__ uac = d.Uf + ((int64_t)ga * v + gc) * oo;
             const float t1ci = __ldg(t1c + pi), t1cj = __ldg(t1c + pj);
             const float ubcij = __ldg(ubc + pi * op + pj), uacij = __ldg(uac + pi * op + pj);
             const float4 ubcj = ld4(ubc + pj * op + pk0), ubci = ld4(ubc + pi * op + pk0);
@@ -569,21 +671,21 @@ __device__ __forceinline__ void energy_chunk(const float (&R)[N], const EDesc &d
 // k values of one c) at a time in rolled loops: a small loop body, and
 // registers free for the FP64 work.  All lanes take part in every TMEM load.
 template <int NA>
-__device__ __forceinline__ void energy_tmem(uint32_t th, const EDesc &d, const SplitParams &p, int part, int b,
-                                            int i, int j, double &e1, double &est) {
+__device__ __forceinline__ void energy_tmem(uint32_t th, const EDesc &d, int part, int b, int i, int j, double &e1,
+                                            double &est) {
     const bool row_ok = b < d.nv[1] && i < d.nv[3] && j < d.nv[4];
-    const int op = p.op;
-    const int64_t v = p.nvir, oo = (int64_t)op * op;
+    const int op = d.op;
+    const int64_t v = d.nvir, oo = (int64_t)op * op;
     const int gb = d.g[1] + b, gi = d.g[3] + i, gj = d.g[4] + j;
     const int pi = d.gp[3] + i, pj = d.gp[4] + j, pk0 = d.gp[5];
     const int nc = d.nv[2], nk = d.nv[5], gc0 = d.g[2], gk0 = d.g[5];
-    const double *__restrict__ eo = p.evl;
-    const double *__restrict__ ev = p.evl + p.nocc;
+    const double *__restrict__ eo = d.eo;
+    const double *__restrict__ ev = d.ev;
     double P[4];
     const double eij = row_ok ? __ldg(eo + gi) + __ldg(eo + gj) : 0.0;
 #pragma unroll
     for (int k = 0; k < 4; ++k) P[k] = (row_ok && k < nk) ? eij + __ldg(eo + gk0 + k) : 0.0;
-    const float *__restrict__ t1b = p.T1f + (int64_t)(row_ok ? gb : 0) * op;
+    const float *__restrict__ t1b = d.T1f + (int64_t)(row_ok ? gb : 0) * op;
     const float t1bi = row_ok ? __ldg(t1b + pi) : 0.f, t1bj = row_ok ? __ldg(t1b + pj) : 0.f;
     const float4 t1bk = row_ok ? ld4(t1b + pk0) : make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll 1
@@ -591,8 +693,8 @@ __device__ __forceinline__ void energy_tmem(uint32_t th, const EDesc &d, const S
         const int a = NA * part + A;
         const bool ok_a = row_ok && a < d.nv[0];
         const int ga = d.g[0] + a;
-        const float *__restrict__ t1a = p.T1f + (int64_t)(ok_a ? ga : 0) * op;
-        const float *__restrict__ uab = p.Uf + ((int64_t)(ok_a ? ga : 0) * v + (ok_a ? gb : 0)) * oo;
+        const float *__restrict__ t1a = d.T1f + (int64_t)(ok_a ? ga : 0) * op;
+        const float *__restrict__ uab = d.Uf + ((int64_t)(ok_a ? ga : 0) * v + (ok_a ? gb : 0)) * oo;
         float t1ai = 0.f, t1aj = 0.f, uabij = 0.f;
         float4 t1ak = make_float4(0.f, 0.f, 0.f, 0.f), uabj = t1ak, uabi = t1ak;
         double eab = 0.0;
@@ -610,9 +712,9 @@ __device__ __forceinline__ void energy_tmem(uint32_t th, const EDesc &d, const S
             const float4 x4 = tc::tmem_ld4(th + (uint32_t)(32 * A + 4 * c));  // every lane
             if (!ok_a || c >= nc) continue;
             const int gc = gc0 + c;
-            const float *__restrict__ t1c = p.T1f + (int64_t)gc * op;
-            const float *__restrict__ ubc = p.Uf + ((int64_t)gb * v + gc) * oo;
-            const float *__restrict__ uac = p.Uf + ((int64_t)ga * v + gc) * oo;
+            const float *__restrict__ t1c = d.T1f + (int64_t)gc * op;
+            const float *__restrict__ ubc = d.Uf + ((int64_t)gb * v + gc) * oo;
+            const float *__restrict__ uac = d.Uf + ((int64_t)ga * v + gc) * oo;
             const float t1ci = __ldg(t1c + pi), t1cj = __ldg(t1c + pj);
             const float ubcij = __ldg(ubc + pi * op + pj), uacij = __ldg(uac + pi * op + pj);
             const float4 ubcj = ld4(ubc + pj * op + pk0), ubci = ld4(ubc + pi * op + pk0);
@@ -649,8 +751,7 @@ __device__ __forceinline__ void energy_tmem(uint32_t th, const EDesc &d, const S
 // so both work-unit shapes give the same bits.
 template <int EPI, int NQ>
 __device__ __forceinline__ void write_partial(double (&e1)[NQ], double (&est)[NQ], double *red, const EDesc &d,
-                                              const SplitParams &p, int quarter0, int quadrant, int lane,
-                                              bool leader) {
+                                              int quarter0, int quadrant, int lane, bool leader) {
 #pragma unroll
     for (int q = 0; q < NQ; ++q) {
         const double x = warp_sum(e1[q]), y = warp_sum(est[q]);
@@ -669,9 +770,20 @@ __device__ __forceinline__ void write_partial(double (&e1)[NQ], double (&est)[NQ
             s1 += red[2 * w];
             s2 += red[2 * w + 1];
         }
-        const double et = d.factor * s1 * p.inv_s2;
-        p.part[2 * d.item] = et;
-        p.part[2 * d.item + 1] = et + d.factor * s2 * p.inv_s;
+        const double et = d.factor * s1 * d.inv_s2;
+        d.part[2 * d.item] = et;
+        d.part[2 * d.item + 1] = et + d.factor * s2 * d.inv_s;
+    }
+}
+
+// Queue mode, energy leader, after the item's pair is written: counts the
+// job's finished items; the one that finishes the job publishes the launch
+// number to the host (its earlier pair writes are visible first).
+__device__ __forceinline__ void job_item_done(const QueueCtl &q, int slot, int64_t items) {
+    __threadfence();
+    if (atomicAdd(q.done + slot, 1ull) + 1 == (unsigned long long)items) {
+        __threadfence_system();
+        *(volatile int *)(q.last_gen + slot) = q.gen;
     }
 }
 
@@ -679,9 +791,8 @@ __device__ __forceinline__ void write_partial(double (&e1)[NQ], double (&est)[NQ
 // TMEM accumulators; HOLD = 1: the last drain writes it to the upper 256
 // TMEM columns, which the energy warps read 32 columns at a time (their
 // registers stay free for the FP64 work), one accumulator.
-template <int TYPE, int HOLD>
-__global__ void __launch_bounds__(HOLD ? SX_THREADS_H : SX_THREADS, 1)
-    split_fused_kernel(const __grid_constant__ SplitParams p) {
+template <int TYPE, int HOLD, int QUEUE>
+__device__ __forceinline__ void split_body(const SplitParams &gp, const QueueCtl &q) {
     constexpr int EPI = HOLD ? SX_EPI_H : SX_EPI;   // energy threads
     constexpr int NA = HOLD ? 2 : 4;                // a values per energy thread
     constexpr int NB = HOLD ? 1 : 2;
@@ -701,6 +812,8 @@ __global__ void __launch_bounds__(HOLD ? SX_THREADS_H : SX_THREADS, 1)
     volatile int64_t *dr_unit = (volatile int64_t *)(misc + 208);
     volatile int64_t *en_unit = (volatile int64_t *)(misc + 216);
     int *dr_nk = (int *)(misc + 224);              // [9] kept K chunks per term of the drained item
+    volatile int *dr_kseg = (volatile int *)(misc + 264);  // K chunks per drain of the drained item's job
+    int *errp = QUEUE ? q.err : gp.err;
     EDesc *desc = (EDesc *)(misc + 320);
     double *red = (double *)(misc + 512);          // [16 energy warps at most][2]
     const UnitRing ring{(int64_t *)(misc + 768), ufull, uempty};
@@ -737,9 +850,9 @@ __global__ void __launch_bounds__(HOLD ? SX_THREADS_H : SX_THREADS, 1)
     if (warp < 4) {
         asm volatile("setmaxnreg.dec.sync.aligned.u32 %0;" ::"n"(SX_REG_LOW));
         if (warp == 0 && lane == 0)
-            run_producer<TYPE>(p, stages, full, empty, abort, ring);
+            run_producer<TYPE, QUEUE>(gp, q, stages, full, empty, abort, ring);
         else if (warp == 1 && lane == 0)
-            run_mma<TYPE, NB>(p, stages, full, empty, tfull, tempty, drain, tmem, abort, ring);
+            run_mma<TYPE, NB, QUEUE>(gp, q, stages, full, empty, tfull, tempty, drain, tmem, abort, ring);
     } else if (warp < 8) {
         // ---------------- drain warps ----------------
         asm volatile("setmaxnreg.dec.sync.aligned.u32 %0;" ::"n"(SX_REG_DRAIN));
@@ -751,13 +864,17 @@ __global__ void __launch_bounds__(HOLD ? SX_THREADS_H : SX_THREADS, 1)
         bool ok = true;
         for (int n = 0; ok; ++n) {
             if (leader) {
-                const int64_t si = ring_take(ring, n, abort);
-                if (si >= 0) {
+                const int64_t unit = ring_take(ring, n, abort);
+                if (unit >= 0) {
+                    SplitParams lp;
+                    if (QUEUE) load_job(q, (int)(unit >> kSlotShift), lp);
+                    const SplitParams &p = QUEUE ? lp : gp;
                     ItemBox bx;
-                    decode_item(p, si, bx);
+                    decode_item(p, QUEUE ? (unit & kItemMask) : unit, bx);
                     for (int t = 0; t < 9; ++t) dr_nk[t] = term_chunk_count<KE>(p, bx, t);
+                    *dr_kseg = p.kseg;
                 }
-                *dr_unit = si;
+                *dr_unit = unit;
             }
             named_bar(1, SX_DRAIN);
             const int64_t si = *dr_unit;
@@ -768,7 +885,7 @@ __global__ void __launch_bounds__(HOLD ? SX_THREADS_H : SX_THREADS, 1)
             for (int t = 0; t < 9 && ok; ++t) {
                 const int nk = dr_nk[t];
                 int kseg;
-                const int nseg = term_segments(nk, p.kseg, kseg);
+                const int nseg = term_segments(nk, *dr_kseg, kseg);
                 for (int sgi = 0; sgi < nseg; ++sgi, ++sg) {
                     const int buf = sg % NB;
                     const bool first = (t == 0 && sgi == 0);
@@ -816,7 +933,7 @@ __global__ void __launch_bounds__(HOLD ? SX_THREADS_H : SX_THREADS, 1)
         }
         if (leader && !ok) {
             *abort = 1;
-            atomicCAS(p.err, 0, 3);
+            atomicCAS(errp, 0, 3);
         }
     } else {
         // ---------------- energy warps ----------------
@@ -824,14 +941,15 @@ __global__ void __launch_bounds__(HOLD ? SX_THREADS_H : SX_THREADS, 1)
         const int et = threadIdx.x - 256;
         const int mm = et & 127, half = et >> 7;  // half: the part of the a range (a = NA*half + A)
         const int rb = mm >> 4, ri = (mm >> 2) & 3, rj_ = mm & 3;  // thread row (b;i,j)
-        const int ew = et >> 5;
         const bool leader = (et == 0);
         float R[HOLD ? 1 : 128];
         constexpr int NQ = HOLD ? 1 : 2;  // quarter partials per thread
         double e1[NQ], est[NQ];
 #pragma unroll
-        for (int q = 0; q < NQ; ++q) e1[q] = est[q] = 0.0;
+        for (int x = 0; x < NQ; ++x) e1[x] = est[x] = 0.0;
         const int quarter0 = HOLD ? half : 2 * half;
+        int slot = 0;            // queue mode, leader: the current item's job slot and item count
+        int64_t job_items = 0;
         for (int n = 0;; ++n) {
             if (leader) {
                 int64_t si = ring_take(ring, n, abort);
@@ -839,8 +957,15 @@ __global__ void __launch_bounds__(HOLD ? SX_THREADS_H : SX_THREADS, 1)
                 if (si >= 0) {
                     w = tc::mbar_wait(xready, n & 1, kWaitNs, abort);
                     if (w) {
+                        SplitParams lp;
+                        if (QUEUE) {
+                            slot = (int)(si >> kSlotShift);
+                            load_job(q, slot, lp);
+                        }
+                        const SplitParams &p = QUEUE ? lp : gp;
+                        job_items = p.n_items;
                         ItemBox bx;
-                        decode_item(p, si, bx);
+                        decode_item(p, QUEUE ? (si & kItemMask) : si, bx);
 #pragma unroll
                         for (int dd = 0; dd < 6; ++dd) {
                             desc->g[dd] = bx.start[dd] + bx.boff[dd];
@@ -849,11 +974,20 @@ __global__ void __launch_bounds__(HOLD ? SX_THREADS_H : SX_THREADS, 1)
                         }
                         desc->factor = p.factor[bx.tq];
                         desc->item = bx.item;
+                        desc->op = p.op;
+                        desc->T1f = p.T1f;
+                        desc->Uf = p.Uf;
+                        desc->eo = p.evl;
+                        desc->ev = p.evl + p.nocc;
+                        desc->part = p.part;
+                        desc->inv_s = p.inv_s;
+                        desc->inv_s2 = p.inv_s2;
+                        desc->nvir = p.nvir;
                     }
                 }
                 if (!w) {
                     *abort = 1;
-                    atomicCAS(p.err, 0, 4);
+                    atomicCAS(errp, 0, 4);
                     si = -2;
                 }
                 *en_unit = si;
@@ -865,11 +999,12 @@ __global__ void __launch_bounds__(HOLD ? SX_THREADS_H : SX_THREADS, 1)
                 // the sub-box is in the hold columns: this warp's lane quadrant, columns 32*(NA*half + A)
                 tc::tc_fence_after();
                 const uint32_t th = tmem + ((uint32_t)((warp & 3) * 32) << 16) + 256u + (uint32_t)(32 * NA * half);
-                if (d.item >= 0) energy_tmem<NA>(th, d, p, half, rb, ri, rj_, e1[0], est[0]);
+                if (d.item >= 0) energy_tmem<NA>(th, d, half, rb, ri, rj_, e1[0], est[0]);
                 tc::tc_fence_before();
                 named_bar(2, EPI);
                 if (leader) tc::mbar_arrive(xfree);  // the hold columns are free
-                if (d.item >= 0) write_partial<EPI, NQ>(e1, est, red, d, p, quarter0, warp & 3, lane, leader);
+                if (d.item >= 0) write_partial<EPI, NQ>(e1, est, red, d, quarter0, warp & 3, lane, leader);
+                if (QUEUE && leader) job_item_done(q, slot, job_items);
             } else {
 #pragma unroll
                 for (int A = 0; A < 4; ++A)
@@ -880,11 +1015,12 @@ __global__ void __launch_bounds__(HOLD ? SX_THREADS_H : SX_THREADS, 1)
                 named_bar(2, EPI);
                 if (leader) tc::mbar_arrive(xfree);
                 if (d.item >= 0) {  // a box outside the tuple has no item
-                    energy_chunk<0, 0, 128>(R, d, p, half, rb, ri, rj_, e1[0], est[0]);
-                    energy_chunk<1, 32, 128>(R, d, p, half, rb, ri, rj_, e1[0], est[0]);
-                    energy_chunk<2, 64, 128>(R, d, p, half, rb, ri, rj_, e1[NQ - 1], est[NQ - 1]);
-                    energy_chunk<3, 96, 128>(R, d, p, half, rb, ri, rj_, e1[NQ - 1], est[NQ - 1]);
-                    write_partial<EPI, NQ>(e1, est, red, d, p, quarter0, warp & 3, lane, leader);
+                    energy_chunk<0, 0, 128>(R, d, half, rb, ri, rj_, e1[0], est[0]);
+                    energy_chunk<1, 32, 128>(R, d, half, rb, ri, rj_, e1[0], est[0]);
+                    energy_chunk<2, 64, 128>(R, d, half, rb, ri, rj_, e1[NQ - 1], est[NQ - 1]);
+                    energy_chunk<3, 96, 128>(R, d, half, rb, ri, rj_, e1[NQ - 1], est[NQ - 1]);
+                    write_partial<EPI, NQ>(e1, est, red, d, quarter0, warp & 3, lane, leader);
+                    if (QUEUE && leader) job_item_done(q, slot, job_items);
                 }
             }
         }
@@ -895,6 +1031,22 @@ __global__ void __launch_bounds__(HOLD ? SX_THREADS_H : SX_THREADS, 1)
         tc::tc_fence_after();
         tc::tmem_dealloc(tmem, 512);
     }
+}
+
+// One job's items (a plan group).
+template <int TYPE, int HOLD>
+__global__ void __launch_bounds__(HOLD ? SX_THREADS_H : SX_THREADS, 1)
+    split_fused_kernel(const __grid_constant__ SplitParams p) {
+    const QueueCtl none{};
+    split_body<TYPE, HOLD, 0>(p, none);
+}
+
+// The shared queue of several jobs' items (serving): resident until the
+// queue stays empty for idle_ns or close is set.
+template <int TYPE, int HOLD>
+__global__ void __launch_bounds__(HOLD ? SX_THREADS_H : SX_THREADS, 1)
+    split_queue_kernel(const __grid_constant__ QueueCtl q) {
+    split_body<TYPE, HOLD, 1>(q.table[0], q);
 }
 
 // ---------------------------------------------------------------------------
@@ -1269,11 +1421,11 @@ int mixed_grid(sdt_job *j, int shape, int64_t n_items, int *grid) {
     return setup(split_fused_kernel<TM_F16, 0>);
 }
 
-int mixed_launch(sdt_job *j, const LaunchArgs &a, cudaStream_t st) {
+namespace {
+SplitParams job_params(sdt_job *j, const LaunchArgs &a) {
     const Tiling &t = j->t;
-    const int type = j->mixed_type;
-    const int ke = type == TM_F32 ? 8 : 16;
-    SplitParams p;
+    const int ke = j->mixed_type == TM_F32 ? 8 : 16;
+    SplitParams p{};
     for (int k = 0; k < 2 * L_N; ++k) p.blk[k] = (const uint8_t *)j->sp[k];
     p.tile_box = (const int32_t *)(j->tile_box_d + j->tile_box_off);
     p.pair_blk = j->tile_box_d + j->pair_blk_off;
@@ -1302,6 +1454,13 @@ int mixed_launch(sdt_job *j, const LaunchArgs &a, cudaStream_t st) {
     p.err = a.err;
     p.queue = a.queue;
     p.all_k = j->all_k;
+    return p;
+}
+}  // namespace
+
+int mixed_launch(sdt_job *j, const LaunchArgs &a, cudaStream_t st) {
+    const int type = j->mixed_type;
+    const SplitParams p = job_params(j, a);
     const int threads = a.shape == 2 ? SX_THREADS_H : SX_THREADS;
     auto launch = [&](auto kern) -> int {
         kern<<<(unsigned)a.grid, threads, SX_SMEM_ALLOC, st>>>(p);
@@ -1320,6 +1479,60 @@ int mixed_launch(sdt_job *j, const LaunchArgs &a, cudaStream_t st) {
         else rc = launch(split_fused_kernel<TM_F16, 0>);
     }
     return rc;
+}
+
+size_t mixed_job_entry_bytes() { return sizeof(SplitParams); }
+
+int mixed_job_entry(sdt_job *j, const LaunchArgs &a, void *entry) {
+    if (j->mixed_type < 0) return fail(SDT_ERR_STATE, "mixed form: the job's split operands are not prepared");
+    const SplitParams p = job_params(j, a);
+    std::memcpy(entry, &p, sizeof(p));
+    return SDT_OK;
+}
+
+int mixed_queue_prepare(int type, int shape) {
+    auto setup = [](auto kern) {
+        return cuda_check(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, SX_SMEM_ALLOC),
+                          "mixed form: queue kernel smem attribute");
+    };
+    if (shape == 2) {
+        if (type == TM_F32) return setup(split_queue_kernel<TM_F32, 1>);
+        if (type == TM_BF16) return setup(split_queue_kernel<TM_BF16, 1>);
+        return setup(split_queue_kernel<TM_F16, 1>);
+    }
+    if (type == TM_F32) return setup(split_queue_kernel<TM_F32, 0>);
+    if (type == TM_BF16) return setup(split_queue_kernel<TM_BF16, 0>);
+    return setup(split_queue_kernel<TM_F16, 0>);
+}
+
+int mixed_queue_launch(int type, int shape, const QueueArgs &a, int grid, cudaStream_t st) {
+    QueueCtl q;
+    q.table = (const SplitParams *)a.table;
+    q.base = a.base;
+    q.head = a.head;
+    q.tail = a.tail;
+    q.done = a.done;
+    q.first_gen = a.first_gen;
+    q.last_gen = a.last_gen;
+    q.close = a.close;
+    q.err = a.err;
+    q.idle_ns = std::min<unsigned long long>(a.idle_ns, kWaitNs / 2);  // below the roles' own wait limit
+    q.max_jobs = a.max_jobs;
+    q.gen = a.gen;
+    const int threads = shape == 2 ? SX_THREADS_H : SX_THREADS;
+    auto launch = [&](auto kern) -> int {
+        kern<<<(unsigned)grid, threads, SX_SMEM_ALLOC, st>>>(q);
+        count_launch();
+        return cuda_check(cudaGetLastError(), "mixed form: queue kernel");
+    };
+    if (shape == 2) {
+        if (type == TM_F32) return launch(split_queue_kernel<TM_F32, 1>);
+        if (type == TM_BF16) return launch(split_queue_kernel<TM_BF16, 1>);
+        return launch(split_queue_kernel<TM_F16, 1>);
+    }
+    if (type == TM_F32) return launch(split_queue_kernel<TM_F32, 0>);
+    if (type == TM_BF16) return launch(split_queue_kernel<TM_BF16, 0>);
+    return launch(split_queue_kernel<TM_F16, 0>);
 }
 
 }  // namespace sdt

@@ -98,13 +98,23 @@ class _Held:
 
 
 class Server:
-    def __init__(self, budget_bytes: int, slots: int = 4, max_ctas: int = 0, check_ctas: int | None = None):
+    """sdt_server_*: admission against an HBM budget, `slots` jobs in
+    flight.  queue: the precision whose jobs go through the shared device
+    work queue drained by one resident kernel (continuous batching; None
+    turns it off and every job gets its own launches), with work-unit
+    `shape`, `reserve` SMs kept free for loading other jobs and `idle` s
+    of waiting for work before the kernel leaves."""
+
+    def __init__(self, budget_bytes: int, slots: int = 4, max_ctas: int = 0, check_ctas: int | None = None,
+                 queue: int | None = PREC_MIXED_FP16, shape: int = 2, reserve: int = 16, idle: float = 0.2):
         self._lib = _capi.lib()
         h = C.c_void_p()
         _capi.check(self._lib.sdt_server_create(int(budget_bytes), int(slots), int(max_ctas), C.byref(h)),
                     "sdt_server_create")
         self._h = h
-        if check_ctas is not None:   # default: a quarter of the SMs for each deferred FP64 check
+        _capi.check(self._lib.sdt_server_set_queue(h, int(queue or 0), int(shape), int(reserve), float(idle)),
+                    "sdt_server_set_queue")
+        if check_ctas is not None:
             _capi.check(self._lib.sdt_server_set_check_ctas(h, int(check_ctas)), "sdt_server_set_check_ctas")
         self._held: dict[int, _Held] = {}
 
@@ -142,6 +152,18 @@ class Server:
     @property
     def peak_bytes(self) -> int:
         return int(self._lib.sdt_server_peak_bytes(self._h))
+
+    def queue_stats(self) -> dict:
+        st = np.zeros(4, dtype=np.int64)
+        _capi.check(self._lib.sdt_server_queue_stats(self._h, st.ctypes.data_as(_capi.PI64)), "sdt_server_queue_stats")
+        return {"launches": int(st[0]), "jobs": int(st[1]), "max_in_queue": int(st[2]), "in_queue": int(st[3])}
+
+    def launches(self, ticket: int) -> tuple[int, int]:
+        """(launch that took the job's first item, launch that finished its last)."""
+        a, b = C.c_int(), C.c_int()
+        _capi.check(self._lib.sdt_server_job_launches(self._h, int(ticket), C.byref(a), C.byref(b)),
+                    "sdt_server_job_launches")
+        return a.value, b.value
 
     def close(self) -> None:
         if self._h:

@@ -1,6 +1,7 @@
 """GPU tests of the serving loop: every served job's energies are the bits
-of the same job run alone; admitted jobs overlap; the byte budget holds;
-a job larger than the budget is refused; the FP64 check is the FP64 form."""
+of the same job run alone; jobs share the resident kernel's work queue
+(continuous batching) and admitted jobs overlap; the byte budget holds; a
+job larger than the budget is refused; the FP64 check is the FP64 form."""
 import time
 
 import numpy as np
@@ -66,3 +67,66 @@ def test_fp64_check_waits_for_admissible_jobs(cuda_device):
     assert st[0]["ran"] <= st[1]["admitted"] and st[2]["ran"] <= st[0]["finished"]
     mixed, fp64 = _alone(specs[0], files[0], prec)
     assert st[0]["energy"] == mixed and st[0]["fp64"] == fp64
+
+
+def test_queue_jobs_share_one_resident_launch(cuda_device):
+    """Jobs submitted back to back enter the shared work queue while the
+    resident kernel runs: several jobs' items are taken and finished inside
+    one launch, and each job's energies are the bits of the job run alone."""
+    specs = serve.job_stream(4, 1000.0, 21, 10, 14)
+    files = serve.prepare(specs)
+    prec = ng.PREC_MIXED_FP16
+    with serve.Server(40 << 30, slots=4, idle=0.5) as srv:
+        tickets = [srv.submit(s.tiling, f, prec) for s, f in zip(specs, files)]
+        srv.drain(600)
+        st = [srv.status(t) for t in tickets]
+        gens = [srv.launches(t) for t in tickets]
+        stats = srv.queue_stats()
+    assert all(x["state"] == 2 for x in st), [x["msg"] for x in st]
+    assert stats["jobs"] == 4 and stats["in_queue"] == 0
+    assert all(a > 0 and b > 0 for a, b in gens)
+    # at least two jobs whose items were all taken and finished by the same launch
+    same = [a for a, b in gens if a == b]
+    assert len(same) >= 2 and max(same.count(g) for g in same) >= 2, (gens, stats)
+    assert stats["max_in_queue"] >= 2
+    for spec, f, x in zip(specs, files, st):
+        mixed, fp64 = _alone(spec, f, prec)
+        assert x["energy"] == mixed
+        assert x["energy"][1] == pytest.approx(fp64[1], rel=2e-6)
+
+
+def test_queue_kernel_leaves_when_idle_and_comes_back(cuda_device):
+    """The resident kernel leaves after its idle time; a job submitted later
+    starts a new launch and is served the same way."""
+    specs = serve.job_stream(2, 10.0, 23, 8, 10)
+    files = serve.prepare(specs)
+    prec = ng.PREC_MIXED_FP16
+    with serve.Server(40 << 30, slots=2, idle=0.02) as srv:
+        t0 = srv.submit(specs[0].tiling, files[0], prec)
+        srv.drain(600)
+        time.sleep(0.3)                                  # well past the idle time: the kernel has left
+        t1 = srv.submit(specs[1].tiling, files[1], prec)
+        srv.drain(600)
+        st = [srv.status(t0), srv.status(t1)]
+        g0, g1 = srv.launches(t0), srv.launches(t1)
+        stats = srv.queue_stats()
+    assert all(x["state"] == 2 for x in st), [x["msg"] for x in st]
+    assert stats["launches"] >= 2 and g1[0] > g0[1]
+    for spec, f, x in zip(specs, files, st):
+        assert x["energy"] == _alone(spec, f, prec)[0]
+
+
+def test_queue_off_runs_each_job_alone(cuda_device):
+    """With the shared queue turned off every job gets its own launches, and
+    the energies are the same bits."""
+    specs = serve.job_stream(3, 100.0, 25, 8, 12)
+    files = serve.prepare(specs)
+    prec = ng.PREC_MIXED_FP16
+    with serve.Server(40 << 30, slots=2, queue=None) as srv:
+        tickets = [srv.submit(s.tiling, f, prec) for s, f in zip(specs, files)]
+        srv.drain(600)
+        st = [srv.status(t) for t in tickets]
+        stats = srv.queue_stats()
+    assert stats["launches"] == 0 and stats["jobs"] == 0
+    for spec, f, x in zip(specs, files, st):
+        assert x["state"] == 2 and x["energy"] == _alone(spec, f, prec)[0]
