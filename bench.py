@@ -194,6 +194,42 @@ def _errors(m, f) -> dict:
             "E(T)_at_0.05Eh_uEh": rel_t * MOLECULAR_EH * 1e6 if rel_t is not None else None}
 
 
+def extra_reference_gpu(ng, t, files, kl, samples, job) -> dict:
+    """NWChem's own CUDA tile path (sd_t_total.cu, built for sm_103a) on the
+    reference arm's sampled tuples: per tuple the reference driver logic on
+    the host (fetch, sort) and the reference's sd_t_*_cuda_ kernels and
+    compute_en_ on the GPU; wall time per tuple, and each tuple's energies
+    against this library's FP64 form."""
+    from oracle import oracle as orc
+    from oracle import ref_cuda
+    if not ref_cuda.staged():
+        return {"unavailable": "the reference CUDA sources were not staged into oracle/_ref/cuda/ with the build"}
+    try:
+        t0 = time.perf_counter()
+        runner = ref_cuda.TileRunner()
+        build_s = time.perf_counter() - t0
+    except (OSError, RuntimeError) as e:
+        return {"unavailable": f"reference CUDA build failed: {str(e)[-300:]}"}
+    P = orc.Problem(t, *files)
+    ids = np.concatenate(list(samples))
+    runner.tuple_energy(P, [int(x) for x in kl[ids[0], :6]])          # warm-up (pool, module load)
+    wall, fl, rel = 0.0, 0.0, 0.0
+    ours_pt = job.run(kl[ids], per_task=True)[2]
+    for q, i in enumerate(ids):
+        tup = [int(x) for x in kl[i, :6]]
+        t0 = time.perf_counter()
+        e = runner.tuple_energy(P, tup)
+        wall += time.perf_counter() - t0
+        fl += ng.flops(t, kl[i:i + 1])
+        rel = max(rel, float(np.max(np.abs(e - ours_pt[q]) / np.abs(ours_pt[q]))))
+    runner.close()
+    return {"value": fl / wall / 1e12, "unit": "TFLOP/s", "tuples": int(len(ids)), "flops": fl, "wall_s": wall,
+            "build_s": build_s, "max_rel_diff_vs_this_fp64_per_tuple": rel,
+            "what": "src/tce/ccsd_t/sd_t_total.cu + memory.cu (FP64 SIMT kernels) compiled with nvcc for sm_103a, "
+                    "driven per tuple like ccsd_t_gpu.F: host fetch/sort of every sub-block, H2D copy, kernel, "
+                    "compute_en_; the oracle's host driver stands in for the Fortran driver"}
+
+
 def extra_molecular(ng, t, kl, ids, e_nat) -> dict:
     """One step of the o=40/v=300 workload with every input scaled so that
     the step's |E(T)| is 0.05 Eh: FP64 and each mixed form, absolute errors."""
@@ -346,7 +382,7 @@ def ours(args) -> None:  # noqa: C901
     lib = _capi.lib()
     lib.sdt_set_error_mode(1)
     extras = set() if args.extras == "none" else (
-        {"o64", "serve", "mol"} if args.extras == "all" else set(args.extras.split(",")))
+        {"o64", "serve", "mol", "refgpu"} if args.extras == "all" else set(args.extras.split(",")))
     if ws > 1:
         extras = set()
 
@@ -481,9 +517,12 @@ def ours(args) -> None:  # noqa: C901
                          "frac": ach / bf16[0], "peak_source": bf16[1], "split_ceiling": ceiling,
                          "frac_of_split_ceiling": ach / ceiling},
         }
-    job.close()
 
     cpu = None
+    extra = {}
+    if rank == 0 and "refgpu" in extras:
+        extra["reference_gpu"] = extra_reference_gpu(ng, t, files, kl, samp[args.warmup:args.warmup + 3], job)
+    job.close()
     if rank == 0 and ws == 1 and not args.no_cpu:
         from oracle import oracle as orc
         cores = os.cpu_count() or 1
@@ -499,7 +538,6 @@ def ours(args) -> None:  # noqa: C901
                          "ccsd_t_kernels_omp.F + drivers"}
         del P
 
-    extra = {}
     if rank == 0 and "mol" in extras:
         extra["molecular_scale"] = extra_molecular(ng, t, kl, step_ids[args.warmup], energies[0])
     files = None                       # the o=64/v=512 inputs need the host memory
