@@ -260,6 +260,12 @@ int sdt_plan_capture(sdt_plan *plan, void *stream);
 int sdt_plan_run(sdt_plan *plan, void *stream, double *energy,
                  double *per_task);
 int sdt_plan_destroy(sdt_plan *plan);
+/* The per-item (E[T], E(T)) pairs of the plan's last run (factor
+ * included), n = sdt_plan_items: items in tuple order (the plan's order for
+ * a single work-unit shape), each tuple's sub-boxes with the h3 box fastest
+ * and the p4 box slowest (4-wide boxes in the FP64 form; 8-wide particle
+ * boxes in the mixed forms).  For checks of parts of a tuple. */
+int sdt_plan_item_energies(sdt_plan *plan, double *pairs, int64_t n);
 /* Sub-box work items of a plan. */
 int64_t sdt_plan_items(const sdt_plan *plan);
 

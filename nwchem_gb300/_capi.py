@@ -75,6 +75,7 @@ def _declare(lib):
         "sdt_server_drain": (C.c_int, [C.c_void_p, C.c_double]),
         "sdt_server_cancel": (C.c_int, [C.c_void_p, C.c_int64]),
         "sdt_server_set_check_ctas": (C.c_int, [C.c_void_p, C.c_int]),
+        "sdt_plan_item_energies": (C.c_int, [C.c_void_p, PD, C.c_int64]),
         "sdt_server_set_queue": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_double]),
         "sdt_server_queue_stats": (C.c_int, [C.c_void_p, PI64]),
         "sdt_server_job_launches": (C.c_int, [C.c_void_p, C.c_int64, C.POINTER(C.c_int), C.POINTER(C.c_int)]),

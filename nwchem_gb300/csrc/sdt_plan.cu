@@ -346,6 +346,15 @@ extern "C" int sdt_plan_destroy(sdt_plan *plan) {
 
 extern "C" int64_t sdt_plan_items(const sdt_plan *plan) { return plan ? plan->items : -1; }
 
+extern "C" int sdt_plan_item_energies(sdt_plan *plan, double *pairs, int64_t n) {
+    if (!plan || !pairs || n != plan->items) return fail(SDT_ERR_ARG, "sdt_plan_item_energies: bad argument");
+    cudaStream_t st = plan->job->stream;
+    int rc = cuda_check(cudaMemcpyAsync(pairs, plan->part_d, 2 * n * sizeof(double), cudaMemcpyDeviceToHost, st),
+                        "sdt_plan_item_energies");
+    if (!rc) rc = cuda_check(cudaStreamSynchronize(st), "sdt_plan_item_energies");
+    return rc;
+}
+
 extern "C" int sdt_job_run(sdt_job *j, const int64_t *klist, int64_t n, int precision, double *energy,
                            double *per_task, void *stream) {
     if (!j || !energy || (n > 0 && !klist)) return fail(SDT_ERR_ARG, "sdt_job_run: null argument");

@@ -228,6 +228,13 @@ class Plan:
     def items(self) -> int:
         return int(self._lib.sdt_plan_items(self._h))
 
+    def item_energies(self) -> np.ndarray:
+        """(items, 2) per-item (E[T], E(T)) pairs of the last run."""
+        out = np.zeros((self.items, 2))
+        _capi.check(self._lib.sdt_plan_item_energies(self._h, out.ctypes.data_as(_capi.PD), self.items),
+                    "sdt_plan_item_energies")
+        return out
+
     def capture(self, stream=None) -> None:
         _capi.check(self._lib.sdt_plan_capture(self._h, _stream_ptr(stream)), "sdt_plan_capture")
 

@@ -242,6 +242,29 @@ def flops(tiling, klist: np.ndarray) -> float:
     return float(lib().orc_tasks_flops(C.byref(p.ts), _pi(kl), len(kl)))
 
 
+def slab_retiling(occ, vir, tup, cut_p4: int, cut_h1: int):
+    """(occ, vir, tuple) of the same orbital spaces re-tiled so that the
+    first cut_p4 orbitals of the tuple's p4 tile and the first cut_h1 of its
+    h1 tile are tiles of their own, and the tuple of those two tiles with
+    the tuple's other tiles.  Its triples elements are the original tuple's
+    elements with p4 < cut_p4 and h1 < cut_h1 (the amplitudes are functions
+    of the orbital indices, and the contractions still run over every
+    orbital), and its multiplicity factor is the original's when neither
+    tile repeats in the tuple, so its energy is the energy of that slab of
+    the original tuple.  Tiles are 1-based, occupied first."""
+    occ, vir = [int(x) for x in occ], [int(x) for x in vir]
+    noab = len(occ)
+    p4, h1 = tup[0] - noab - 1, tup[3] - 1
+    if tup[0] in tup[1:3] or tup[3] in tup[4:6]:
+        raise ValueError("the p4 and h1 tiles must not repeat in the tuple")
+    occ2 = occ[:h1] + [cut_h1, occ[h1] - cut_h1] + occ[h1 + 1:]
+    vir2 = vir[:p4] + [cut_p4, vir[p4] - cut_p4] + vir[p4 + 1:]
+    no2 = len(occ2)
+    omap = lambda b: b + (1 if b - 1 > h1 else 0)
+    vmap = lambda b: no2 + (b - noab) + (1 if b - noab - 1 > p4 else 0)
+    return occ2, vir2, [vmap(tup[0]), vmap(tup[1]), vmap(tup[2]), omap(tup[3]), omap(tup[4]), omap(tup[5])]
+
+
 def kernel(family: str, k: int, dims_fortran, triplesx: np.ndarray, a: np.ndarray, b: np.ndarray) -> None:
     """One oracle tile kernel, Fortran CPU dialect dims (h3d,h2d,h1d,p6d,p5d,p4d[,k7d])."""
     f = getattr(lib(), f"orc_sd_t_{family}")

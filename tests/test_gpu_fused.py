@@ -313,3 +313,39 @@ def test_per_tuple_output_writes_only_its_pairs(gpu):
             assert lib.sdt_plan_run(p._h, None, e.ctypes.data_as(_capi.PD), pt.ctypes.data_as(_capi.PD)) == 0
             assert np.all(np.isnan(pt[2 * n:])) and np.all(np.isnan(e[2:]))
             assert np.array_equal(pt[:2 * n].reshape(n, 2), ref[2])
+
+
+def test_fused_o64_shaped_tuple_slab(gpu):
+    """A tuple of the o=64/v=512 workload's shape -- 64x64x64 particle and
+    32x32x32 hole tiles, 8.6e9 triples elements, 2.1e6 sub-boxes -- with the
+    contraction length cut to o + v = 256 (o=64 as 2x32, v=192 as 3x64, seed
+    2).  The FP64 form's per-item energies over the slab p4 < 4, h1 < 4 (the
+    first p4 box and h1 box) against the oracle's energy of that slab,
+    evaluated as a tuple of the re-tiled orbital space, to 1e-10."""
+    occ, vir = [32, 32], [64, 64, 64]
+    t = ng.Tiling(occ, vir).with_evl(2)
+    files = ng.synth_inputs(t, 2)
+    kl = ng.task_list(t)
+    row = next(k for k in kl if list(k[:6]) == [3, 4, 5, 1, 2, 2])
+    with ng.TriplesJob(t) as job:
+        job.load(*files)
+        with ng.Plan(job, row[None, :]) as p:
+            e = p.run()
+            items = p.item_energies()
+    nb = [16, 16, 16, 8, 8, 8]
+    assert len(items) == int(np.prod(nb))
+    idx = np.arange(len(items))
+    box = []
+    for n in reversed(nb):
+        box.append(idx % n)
+        idx //= n
+    box = box[::-1]                                            # p4, p5, p6, h1, h2, h3 boxes
+    slab = items[(box[0] == 0) & (box[3] == 0)].sum(axis=0)
+    assert items.sum(axis=0)[1] == pytest.approx(e[1], rel=1e-12)
+    occ2, vir2, new = orc.slab_retiling(occ, vir, [3, 4, 5, 1, 2, 2], 4, 4)
+    t2 = ng.Tiling(occ2, vir2).with_evl(2)
+    P2 = orc.Problem(t2, *ng.synth_inputs(t2, 2))
+    kl2 = P2.task_list()
+    q = next(i for i, k in enumerate(kl2) if list(k[:6]) == new)
+    _, _, pt, _ = P2.ccsd_t(kl2, task_ids=np.array([q]))
+    assert slab[0] == pytest.approx(pt[0, 0], rel=REL) and slab[1] == pytest.approx(pt[0, 1], rel=REL)

@@ -184,3 +184,33 @@ def test_oracle_workload_inputs_equal_the_library():
     o = orc.Tiling([3, 2, 3], [4, 5, 4, 3], [0, 1, 1], [1, 0, 1, 0], seed=5)
     for x, y in zip(orc.synth_inputs(o, 5), ng.synth_inputs(t, 5)):
         assert np.array_equal(x.hash, y.hash) and np.array_equal(x.data, y.data)
+
+
+def test_slab_retiling_is_exact_on_the_oracle():
+    """CPU check of the slab method the GPU test of the o=64-shaped tuple
+    uses: the energy of the re-tiled tuple equals the slab p4 < 3, h1 < 2 of
+    the original tuple, summed from the oracle's full triples tiles."""
+    occ, vir = [6, 5], [7, 6, 8]
+    t = ng.Tiling(occ, vir).with_evl(12)
+    P = orc.Problem(t, *ng.synth_inputs(t, 12))
+    tup = [3, 4, 5, 1, 2, 2]
+    s, d = P.tuple_tiles(tup)                                  # (h3,h2,h1,p6,p5,p4)
+    r, off = t.range, t.offset
+    ev = [t.evl[off[b - 1]:off[b - 1] + r[b - 1]] for b in tup]   # p4,p5,p6,h1,h2,h3
+    D = (ev[5][:, None, None, None, None, None] + ev[4][None, :, None, None, None, None]
+         + ev[3][None, None, :, None, None, None] - ev[2][None, None, None, :, None, None]
+         - ev[1][None, None, None, None, :, None] - ev[0][None, None, None, None, None, :])
+    sl = (slice(None), slice(None), slice(0, 2), slice(None), slice(None), slice(0, 3))
+    f = 0.5                                                    # h2 = h3 tile
+    e1 = f * np.sum(d[sl] ** 2 / D[sl])
+    e2 = f * np.sum(d[sl] * (d[sl] + s[sl]) / D[sl])
+    occ2, vir2, new = orc.slab_retiling(occ, vir, tup, 3, 2)
+    t2 = ng.Tiling(occ2, vir2).with_evl(12)
+    P2 = orc.Problem(t2, *ng.synth_inputs(t2, 12))
+    s2, d2 = P2.tuple_tiles(new)
+    # the same elements; the contraction over the re-tiled virtual space is summed in other pieces
+    assert np.allclose(d2, d[sl], rtol=0, atol=1e-14 * np.abs(d).max()) and np.array_equal(s2, s[sl])
+    kl2 = P2.task_list()
+    q = next(i for i, k in enumerate(kl2) if list(k[:6]) == new)
+    _, _, pt, _ = P2.ccsd_t(kl2, task_ids=np.array([q]))
+    assert pt[0, 0] == pytest.approx(e1, rel=1e-12) and pt[0, 1] == pytest.approx(e2, rel=1e-12)
