@@ -545,7 +545,11 @@ void monitor(sdt_server *s) {
 void run_check(sdt_server *s, sdt_server::Job *job) {
     cudaSetDevice(s->device);
     const int64_t n = (int64_t)job->kl.size() / 7;
-    sdt_job_set_sm_exclusive(job->held, s->check_ctas > 0);  // exactly check_ctas SMs; 0: all of them
+    // Without the shared queue a check takes exactly check_ctas SMs (one CTA each) and mixed jobs
+    // launch on the others.  With it, the resident kernel holds all but the reserved SMs, so the
+    // check gets check_ctas SMs' worth of CTAs (four per SM) on the free ones, where they share the
+    // SMs with other jobs' loading kernels.
+    sdt_job_set_sm_exclusive(job->held, s->check_ctas > 0 && !s->use_queue);
     sdt_job_set_max_ctas(job->held, s->check_ctas);
     const int rc = sdt_job_run(job->held, job->kl.data(), n, SDT_PREC_FP64, job->f, nullptr, nullptr);
     if (rc) {
