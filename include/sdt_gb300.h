@@ -300,8 +300,10 @@ int sdt_server_submit(sdt_server *server, const sdt_tiling *t,
 int sdt_server_status(sdt_server *server, int64_t ticket, int *state,
                       double *energy, double *fp64, double *times,
                       char *msg, size_t len);
-/* CTAs (one per SM) of each deferred FP64 check (default half the SMs the
- * shared queue leaves free, or a quarter of the SMs without the queue). */
+/* SMs (one CTA each) of each deferred FP64 check: default half the SMs the
+ * shared queue leaves free (with the queue: 1 to reserve_sms, one check at
+ * a time, so the resident kernel never waits for a check's SMs), or a
+ * quarter of the SMs without the queue. */
 int sdt_server_set_check_ctas(sdt_server *server, int ctas);
 /* The shared queue: its precision (SDT_PREC_FP64 turns it off), work-unit
  * shape (1 or 2, as sdt_job_set_mixed_shape; default 2), SMs kept free of

@@ -545,11 +545,10 @@ void monitor(sdt_server *s) {
 void run_check(sdt_server *s, sdt_server::Job *job) {
     cudaSetDevice(s->device);
     const int64_t n = (int64_t)job->kl.size() / 7;
-    // Without the shared queue a check takes exactly check_ctas SMs (one CTA each) and mixed jobs
-    // launch on the others.  With it, the resident kernel holds all but the reserved SMs, so the
-    // check gets check_ctas SMs' worth of CTAs (four per SM) on the free ones, where they share the
-    // SMs with other jobs' loading kernels.
-    sdt_job_set_sm_exclusive(job->held, s->check_ctas > 0 && !s->use_queue);
+    // A check takes exactly check_ctas SMs (one CTA each).  With the shared queue those are part
+    // of the SMs the resident kernel leaves free, so the kernel never waits for SMs a check holds
+    // (a check runs for seconds) -- one check at a time, check_ctas <= reserve.
+    sdt_job_set_sm_exclusive(job->held, s->check_ctas > 0);
     sdt_job_set_max_ctas(job->held, s->check_ctas);
     const int rc = sdt_job_run(job->held, job->kl.data(), n, SDT_PREC_FP64, job->f, nullptr, nullptr);
     if (rc) {
@@ -571,7 +570,10 @@ void worker(sdt_server *s) {
         return !s->queue.empty() &&
                (!s->adm.fits_ever(s->queue.front()->bytes) || s->adm.can_admit(s->queue.front()->bytes));
     };
-    auto check_ready = [&] { return !s->checks.empty() && s->adm.busy < s->adm.slots && !head_ready(); };
+    auto check_ready = [&] {
+        return !s->checks.empty() && s->adm.busy < s->adm.slots && !head_ready() &&
+               (!s->use_queue || s->checks_running == 0);
+    };
     while (true) {
         s->cv.wait(lk, [&] { return s->stop || head_ready() || check_ready(); });
         if (s->stop) return;
@@ -706,6 +708,8 @@ extern "C" int sdt_server_job_launches(sdt_server *s, int64_t ticket, int *first
 extern "C" int sdt_server_set_check_ctas(sdt_server *s, int ctas) {
     if (!s || ctas < 0) return fail(SDT_ERR_ARG, "sdt_server_set_check_ctas: bad argument");
     std::lock_guard<std::mutex> lk(s->mu);
+    if (s->use_queue && (ctas < 1 || ctas > s->q.reserve))
+        return fail(SDT_ERR_ARG, "sdt_server_set_check_ctas: with the shared queue, 1 to reserve SMs");
     s->check_ctas = s->sms > 0 ? std::min(ctas, s->sms - 1) : ctas;
     return SDT_OK;
 }

@@ -26,7 +26,7 @@ def test_served_jobs_match_alone_and_overlap(cuda_device):
     prec = ng.PREC_MIXED_FP16
     need = [serve.job_bytes(s.tiling, prec) for s in specs]
     budget = int(sum(sorted(need)[-3:]))              # room for about three jobs at a time
-    with serve.Server(budget, slots=3) as srv:
+    with serve.Server(budget, slots=3, reserve=40, check_ctas=32) as srv:
         tickets = [srv.submit(s.tiling, f, prec, check_fp64=(s.id % 4 == 0)) for s, f in zip(specs, files)]
         srv.drain(600)
         st = [srv.status(t) for t in tickets]
@@ -59,7 +59,7 @@ def test_fp64_check_waits_for_admissible_jobs(cuda_device):
     specs = serve.job_stream(3, 100.0, 5, 16, 16)  # jobs of some ms: all three are queued before the first ends
     files = serve.prepare(specs)
     prec = ng.PREC_MIXED_FP16
-    with serve.Server(40 << 30, slots=1) as srv:
+    with serve.Server(40 << 30, slots=1, reserve=40, check_ctas=32) as srv:
         tickets = [srv.submit(s.tiling, f, prec, check_fp64=(s.id == 0)) for s, f in zip(specs, files)]
         srv.drain(600)
         st = [srv.status(t) for t in tickets]
