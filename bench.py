@@ -299,7 +299,7 @@ def extra_o64v512(ng, stream, bf16) -> dict:
 
 
 def serve_stream(ng, jobs: int, rate: float, omin: int, omax: int, slots: int, check_every: int,
-                 max_ctas: int = 0, queue: bool = True) -> dict:
+                 max_ctas: int = 0, queue: bool = True, reserve: int = 16) -> dict:
     """Serving stream: Poisson arrivals at `rate` jobs/s, o ~ U{omin..omax},
     v = round(o * U[5,8]), tiles from {8..32} / {16..64} (no irreps), inputs
     seeded with the job id; FIFO admission against a 150 GB HBM budget with
@@ -318,7 +318,8 @@ def serve_stream(ng, jobs: int, rate: float, omin: int, omax: int, slots: int, c
     prec = ng.PREC_MIXED_FP16
     budget = 150 * 10**9
     check = [check_every > 0 and s.id % check_every == 0 for s in specs]
-    with serve.Server(budget, slots=slots, max_ctas=max_ctas, queue=prec if queue else None) as srv:
+    with serve.Server(budget, slots=slots, max_ctas=max_ctas, queue=prec if queue else None,
+                      reserve=reserve) as srv:
         w = srv.submit(specs[0].tiling, files[0], prec)       # warm-up job, not counted
         srv.drain(600)
         srv.status(w)
@@ -353,7 +354,8 @@ def serve_stream(ng, jobs: int, rate: float, omin: int, omax: int, slots: int, c
     return {
         "workload": f"serving: {jobs} jobs, Poisson {rate:g} jobs/s, o ~ U{{{omin}..{omax}}}, "
                     f"v = round(o*U[5,8]), tiles {{8..32}}/{{16..64}}, seed = job id",
-        "continuous_batching": queue, "slots": slots, "budget_bytes": budget, "peak_admitted_bytes": peak,
+        "continuous_batching": queue, "slots": slots, "reserve_sms": reserve if queue else None,
+        "budget_bytes": budget, "peak_admitted_bytes": peak,
         "jobs_done": len(ok), "jobs_failed": len(st) - len(ok),
         "jobs_per_s": len(ok) / span, "span_s": span, "p50_latency_s": float(np.percentile(lat, 50)),
         "p99_latency_s": float(np.percentile(lat, 99)), "mean_latency_s": float(lat.mean()),
@@ -745,7 +747,7 @@ def workload_serve(args) -> None:
     import nwchem_gb300 as ng
     torch.cuda.set_device(0)
     print(json.dumps(serve_stream(ng, args.jobs, args.rate, args.omin, args.omax, args.slots, args.check_every,
-                                  args.max_ctas, queue=not args.no_queue)), flush=True)
+                                  args.max_ctas, queue=not args.no_queue, reserve=args.reserve)), flush=True)
 
 
 def main() -> None:
@@ -768,6 +770,7 @@ def main() -> None:
     ap.add_argument("--check-every", type=int, default=100, help="serve: FP64 check on every n-th job (0: none)")
     ap.add_argument("--max-ctas", type=int, default=0, help="serve, queue off: CTA cap per job launch (0: all SMs)")
     ap.add_argument("--no-queue", action="store_true", help="serve: one launch per job instead of the shared queue")
+    ap.add_argument("--reserve", type=int, default=16, help="serve: SMs the resident kernel leaves free")
     ap.add_argument("--case", default="o40v114", choices=["o40v114", "o64v128", "sym8s"], help="--profile case")
     ap.add_argument("--shape", type=int, default=1, choices=[1, 2], help="mixed work-unit shape")
     ap.add_argument("--mixed", default="", choices=["", "tf32", "bf16", "fp16"],
