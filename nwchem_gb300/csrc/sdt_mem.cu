@@ -32,6 +32,42 @@ std::mutex &pool_mu() {
 }
 cudaStream_t g_stream = nullptr;
 int g_stream_dev = -1;
+cudaStream_t g_alloc_stream = nullptr;
+int g_alloc_dev = -1;
+
+// Device blocks come from the stream-ordered allocator on a stream of their
+// own (then that stream is synchronised, which waits for nothing else).  A
+// plain cudaMalloc is an implicit synchronisation point: work issued after
+// it waits for all work issued before it, so a job loaded while a long
+// kernel runs (a resident serving kernel, an FP64 check) would wait for it.
+cudaError_t dev_alloc(void **p, size_t bytes) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (!g_alloc_stream || g_alloc_dev != dev) {
+        cudaStream_t s = nullptr;
+        if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess) {
+            cudaGetLastError();
+            return cudaMalloc(p, bytes);
+        }
+        g_alloc_stream = s;
+        g_alloc_dev = dev;
+    }
+    cudaError_t e = cudaMallocAsync(p, bytes, g_alloc_stream);
+    if (e == cudaErrorNotSupported) {
+        cudaGetLastError();
+        return cudaMalloc(p, bytes);
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(g_alloc_stream);
+    return e;
+}
+void dev_free(void *p) {
+    if (g_alloc_stream && cudaFreeAsync(p, g_alloc_stream) == cudaSuccess) {
+        cudaStreamSynchronize(g_alloc_stream);
+        return;
+    }
+    cudaGetLastError();
+    cudaFree(p);
+}
 }  // namespace
 
 int cuda_check(cudaError_t e, const char *what) {
@@ -63,15 +99,15 @@ static void *take(std::multimap<size_t, void *> &fl, std::map<void *, size_t> &l
     }
     void *p = nullptr;
     PhaseTrace tr(dev ? "pool: cudaMalloc" : "pool: cudaMallocHost");
-    cudaError_t e = dev ? cudaMalloc(&p, bytes) : cudaMallocHost(&p, bytes);
+    cudaError_t e = dev ? dev_alloc(&p, bytes) : cudaMallocHost(&p, bytes);
     tr.mark(std::to_string(bytes).c_str(), nullptr);
     if (e != cudaSuccess) {
         cudaGetLastError();
         // Drop the cache and retry once.
-        for (auto &kv : fl) dev ? cudaFree(kv.second) : cudaFreeHost(kv.second);
+        for (auto &kv : fl) dev ? dev_free(kv.second) : (void)cudaFreeHost(kv.second);
         fl.clear();
         tr.mark("cache dropped", nullptr);
-        e = dev ? cudaMalloc(&p, bytes) : cudaMallocHost(&p, bytes);
+        e = dev ? dev_alloc(&p, bytes) : cudaMallocHost(&p, bytes);
         if (e != cudaSuccess) {
             cudaGetLastError();
             return nullptr;
