@@ -434,11 +434,15 @@ __device__ __forceinline__ void run_producer(const SplitParams &gp, const QueueC
                     ++g;
                     uint8_t *st = stages + s * SX_STAGE;
                     tc::mbar_arrive_expect_tx(&full[s], SX_STAGE);
+                    // all four source addresses first, then the four copies back to back (the
+                    // single producer thread's issue rate bounds the long-K contractions)
                     const int64_t ab = abase + c, bb = bbase + c;
-                    bulk_load(st, p.blk[2 * la] + ab * SX_A, SX_A, &full[s]);
-                    bulk_load(st + SX_A, p.blk[2 * la + 1] + ab * SX_A, SX_A, &full[s]);
-                    bulk_load(st + 2 * SX_A, p.blk[2 * lb] + bb * SX_B, SX_B, &full[s]);
-                    bulk_load(st + 2 * SX_A + SX_B, p.blk[2 * lb + 1] + bb * SX_B, SX_B, &full[s]);
+                    const uint8_t *ah = p.blk[2 * la] + ab * SX_A, *al = p.blk[2 * la + 1] + ab * SX_A;
+                    const uint8_t *bh = p.blk[2 * lb] + bb * SX_B, *bl = p.blk[2 * lb + 1] + bb * SX_B;
+                    bulk_load(st, ah, SX_A, &full[s]);
+                    bulk_load(st + SX_A, al, SX_A, &full[s]);
+                    bulk_load(st + 2 * SX_A, bh, SX_B, &full[s]);
+                    bulk_load(st + 2 * SX_A + SX_B, bl, SX_B, &full[s]);
                 });
             }
         }
