@@ -29,8 +29,9 @@ struct sdt_job {
     double *arr[sdt::DST_N] = {nullptr};
     size_t arr_n[sdt::DST_N] = {0};
     std::vector<int64_t> pair_host;     // Vd2 region offsets (fp64 elements), -1 if none
-    // mixed form: split operands in block-major layouts (hi at [2*k], lo at
-    // [2*k+1]; fp32 holding TF32 values, or bf16 / fp16), FP32 copies of T1d
+    // mixed form: split operands in block-major layouts (one buffer per
+    // layout at [2*k], each block its hi half then its lo half; [2*k+1]
+    // unused; fp32 holding TF32 values, or bf16 / fp16), FP32 copies of T1d
     // and Ud for the s1 terms, and the box tables
     void *sp[2 * sdt::SP_N] = {nullptr};
     size_t sp_n[2 * sdt::SP_N] = {0};    // bytes
