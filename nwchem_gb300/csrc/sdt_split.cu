@@ -437,7 +437,7 @@ __device__ __forceinline__ void run_producer(const SplitParams &gp, const QueueC
                     ++g;
                     uint8_t *st = stages + s * SX_STAGE;
                     tc::mbar_arrive_expect_tx(&full[s], SX_STAGE);
-                    // all four source addresses first, then the four copies back to back (the
+                    // both source addresses first, then the two copies back to back (the
                     // single producer thread's issue rate bounds the long-K contractions)
                     const int64_t ab = abase + c, bb = bbase + c;
                     const uint8_t *a = p.blk[2 * la] + ab * (2 * SX_A), *b = p.blk[2 * lb] + bb * (2 * SX_B);
