@@ -347,6 +347,12 @@ def serve_stream(ng, jobs: int, rate: float, omin: int, omax: int, slots: int, c
     chk = [x for x, c in zip(st, check) if c and x["state"] == 2]
     errs = [abs(x["energy"][1] - x["fp64"][1]) / abs(x["fp64"][1]) for x in chk if x["fp64"][1] != 0.0]
     aerr = [abs(x["energy"][1] - x["fp64"][1]) for x in chk]
+    worst = int(np.argmax([x["ran"] - x["submitted"] if x["state"] == 2 else -1 for x in st]))
+    wx = st[worst]
+    worst_job = {"id": specs[worst].id, "o": specs[worst].tiling.nocc, "v": specs[worst].tiling.nvir,
+                 "checked": bool(check[worst]), "launches": list(gens[worst]),
+                 **{k: wx[b] - wx[a] for k, a, b in (("queue", "submitted", "admitted"), ("load", "admitted", "loaded"),
+                                                     ("compute", "loaded", "ran"))}}
     shared = {}
     for a, b in gens:
         if a > 0 and a == b:
@@ -364,6 +370,7 @@ def serve_stream(ng, jobs: int, rate: float, omin: int, omax: int, slots: int, c
         "phase_p99_s": {k: float(np.percentile(v, 99)) for k, v in phase.items()},
         "tflops": flops / span / 1e12, "fp64_checked": len(chk), "fp64_checks_done_at_s": checks_done,
         "queue": {**qs, "most_jobs_finished_in_one_launch": max(shared.values()) if shared else 0},
+        "slowest_job": worst_job,
         "max_rel_err_E(T)_vs_fp64": max(errs) if errs else None,
         "max_abs_err_E(T)_vs_fp64_Eh": max(aerr) if aerr else None,
         "input_generation_s": gen_s}

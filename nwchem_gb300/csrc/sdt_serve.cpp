@@ -34,6 +34,7 @@
 #include <algorithm>
 #include <chrono>
 #include <condition_variable>
+#include <cstdio>
 #include <cstring>
 #include <deque>
 #include <memory>
@@ -313,6 +314,7 @@ int queue_reap(sdt_server *s) {
     const cudaError_t e = cudaEventQuery(Q.kev);
     if (e == cudaErrorNotReady) return SDT_OK;
     Q.running = false;
+    if (trace_on()) std::fprintf(stderr, "[sdt trace] t=%.4f queue launch %d ended\n", s->now(), Q.gen);
     int rc = cuda_check(e, "sdt_server: queue kernel");
     int *w = stage_word(Q);
     if (!rc) rc = cuda_check(cudaMemcpyAsync(w, Q.err_d, sizeof(int), cudaMemcpyDeviceToHost, Q.pst), "sdt_server");
@@ -361,6 +363,9 @@ int queue_ensure(sdt_server *s) {
         Q.running = true;
         ++Q.launches;
     }
+    if (trace_on())
+        std::fprintf(stderr, "[sdt trace] t=%.4f queue launch %d (head %llu, tail %llu, jobs in queue %lld)\n",
+                     s->now(), Q.gen, head, Q.tail, (long long)Q.in_flight);
     return rc;
 }
 
@@ -398,6 +403,9 @@ int queue_publish(sdt_server *s, sdt_server::Job *job) {
                                              cudaMemcpyHostToDevice, Q.pst), "sdt_server: publish");
     if (rc) return rc;
     job->slot = slot;
+    if (trace_on())
+        std::fprintf(stderr, "[sdt trace] t=%.4f job %lld appended: slot %d, positions %lld..%llu\n", s->now(),
+                     (long long)job->id, slot, stage_base(Q)[slot], Q.tail);
     Q.by_slot[slot] = job;
     ++Q.in_flight;
     ++Q.jobs;
@@ -463,6 +471,9 @@ bool run_queued(sdt_server *s, sdt_server::Job *job) {
 // its memory is returned (or kept for its FP64 check).
 void queue_finish(sdt_server *s, sdt_server::Job *job, int rc_in) {
     int rc = rc_in;
+    if (trace_on())
+        std::fprintf(stderr, "[sdt trace] t=%.4f job %lld items done (launches %d..%d)\n", s->now(),
+                     (long long)job->id, job->first_gen, job->last_gen);
     if (!rc) rc = plan_finish(job->plan, (cudaStream_t)sdt_job_stream(job->dj), job->e);
     if (rc) {
         job->err = rc;
@@ -550,7 +561,9 @@ void run_check(sdt_server *s, sdt_server::Job *job) {
     // (a check runs for seconds) -- one check at a time, check_ctas <= reserve.
     sdt_job_set_sm_exclusive(job->held, s->check_ctas > 0);
     sdt_job_set_max_ctas(job->held, s->check_ctas);
+    if (trace_on()) std::fprintf(stderr, "[sdt trace] t=%.4f FP64 check of job %lld starts\n", s->now(), (long long)job->id);
     const int rc = sdt_job_run(job->held, job->kl.data(), n, SDT_PREC_FP64, job->f, nullptr, nullptr);
+    if (trace_on()) std::fprintf(stderr, "[sdt trace] t=%.4f FP64 check of job %lld ends\n", s->now(), (long long)job->id);
     if (rc) {
         char buf[512] = {0};
         sdt_last_error(buf, sizeof(buf));
