@@ -142,3 +142,30 @@ def test_held_bytes_never_deadlock_the_queue():
     chk = np.full(n, 0.5)
     start, ready, done = _check_deferred(arr, nb, svc, chk, 100, 4)
     assert np.all(done > 0) and done.max() < 1e3
+
+
+def test_queue_settings_are_checked_without_a_gpu():
+    """sdt_server_set_queue takes a precision, a work-unit shape of 1 or 2,
+    at least one reserved SM and an idle time in (0, 1] s; the statistics
+    start at zero and an unknown ticket is refused."""
+    import ctypes as C
+    import numpy as np
+    from nwchem_gb300 import _capi
+    lib = _capi.lib()
+    lib.sdt_set_error_mode(1)
+    h = C.c_void_p()
+    _capi.check(lib.sdt_server_create(1 << 30, 2, 0, C.byref(h)), "sdt_server_create")
+    try:
+        for args in ((3, 3, 16, 0.2), (3, 2, 0, 0.2), (3, 2, 16, 0.0), (3, 2, 16, 1.5), (7, 2, 16, 0.2)):
+            assert lib.sdt_server_set_queue(h, *args) == 1, args
+            _capi.last_error()
+        assert lib.sdt_server_set_queue(h, 3, 1, 24, 0.5) == 0
+        assert lib.sdt_server_set_queue(h, 0, 2, 16, 0.2) == 0          # FP64: the queue off
+        st = np.full(4, -1, dtype=np.int64)
+        assert lib.sdt_server_queue_stats(h, st.ctypes.data_as(_capi.PI64)) == 0
+        assert st.tolist() == [0, 0, 0, 0]
+        a, b = C.c_int(), C.c_int()
+        assert lib.sdt_server_job_launches(h, 5, C.byref(a), C.byref(b)) == 1
+        _capi.last_error()
+    finally:
+        lib.sdt_server_destroy(h)
