@@ -63,7 +63,8 @@ FP64_DRAM_BYTES_PER_FLOP = (327.9e6 + 26.2e6) / 2.587e11
 MIXED_FORMS = (("tf32", 1), ("bf16", 2), ("fp16", 3))
 MIXED_NOTE = {"tf32": "TF32x3: TF32 hi/lo pairs, kind::tf32", "bf16": "BF16x3: bf16 hi/lo pairs, kind::f16",
               "fp16": "FP16x3: fp16 hi/lo pairs of power-of-two scaled operands, kind::f16",
-              "all": "FP32 accumulation in TMEM; s1 products FP32; denominator, division and energy sums FP64"}
+              "all": "FP32 accumulation in TMEM; s1 products, denominator and quotient FP32 "
+                     "(orbital energies shifted to the gap midpoint); energy sums FP64"}
 MOLECULAR_EH = 0.05       # |E(T)| of a mid-sized molecule, for the absolute-error bound
 
 

@@ -32,7 +32,8 @@ struct sdt_job {
     // mixed form: split operands in block-major layouts (one buffer per
     // layout at [2*k], each block its hi half then its lo half; [2*k+1]
     // unused; fp32 holding TF32 values, or bf16 / fp16), FP32 copies of T1d
-    // and Ud for the s1 terms, and the box tables
+    // and Ud for the s1 terms (the T1 buffer followed by the orbital energies
+    // minus the gap midpoint, FP32), and the box tables
     void *sp[2 * sdt::SP_N] = {nullptr};
     size_t sp_n[2 * sdt::SP_N] = {0};    // bytes
     int mixed_type = -1;                 // TM_* of the prepared copies, -1: none

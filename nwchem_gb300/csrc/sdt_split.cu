@@ -29,8 +29,10 @@
 // finished sub-box from shared memory into registers (128 values per thread)
 // and release it; the drain warps then store the next item's first term into
 // it while the energy warps evaluate the copy: the s1 products in FP32 from
-// FP32 copies of T1 and the vvoo block, then, in FP64, the denominator, the
-// division and the two energy sums.  So the energy work of one item overlaps
+// FP32 copies of T1 and the vvoo block, the denominator and the quotient in
+// FP32 (orbital energies shifted by the midpoint of the occupied-virtual
+// gap, so that no sum in a denominator cancels), and the two energy sums in
+// FP64, one FP64 add per four elements.  So the energy work of one item overlaps
 // the contractions of the next.  In the tensor-memory hold variant (HOLD = 1)
 // the last drain writes the finished sub-box into the upper 256 TMEM columns
 // instead, one accumulator remains, and 16 energy warps read the sub-box
@@ -129,7 +131,7 @@ struct EDesc {
     double factor;  // the tuple's multiplicity factor
     long long item; // the item's index within its job
     const float *T1f, *Uf;      // the job's FP32 copies of T1 and the vvoo block
-    const double *eo, *ev;      // its occupied and virtual orbital energies
+    const float *eo, *ev;       // its occupied and virtual orbital energies, shifted, FP32
     double *part;               // its per-item energy pairs
     double inv_s, inv_s2;       // its operand scaling
     long long nvir;
@@ -158,6 +160,7 @@ struct alignas(16) SplitParams {
     const float *T1f, *Uf;        // FP32 copies: [v][OP], [v][v][OP][OP], holes padded per tile to 4
     int32_t op;                   // OP, the padded hole count (4 x hole boxes)
     const double *evl;
+    const float *evf;             // orbital energies minus the gap midpoint, FP32 (occupied, then virtual)
     const int32_t *tiles;         // [ntiles][4] start, range, spin, sym
     int32_t noab, nvab, nk_o, nk_v, kseg, nob, nvb;
     int64_t nocc, nvir;
@@ -582,8 +585,8 @@ __device__ __forceinline__ void drain_any(int t, bool store, float *X, uint32_t 
 }
 
 // Exact FP32 -> FP64 widening by assembling the IEEE-754 fields on the
-// integer pipes (the conversion instruction runs on the FP64 pipe, which
-// bounds the energy pass): sign kept, exponent rebiased by 1023 - 127,
+// integer pipes (the conversion instruction runs on the narrow FP64 pipe):
+// sign kept, exponent rebiased by 1023 - 127,
 // mantissa shifted into the top 23 of 52 bits; zero and FP32 subnormals
 // (|x| < 2^-126) give signed zero, infinities and NaNs keep their class.
 __device__ __forceinline__ double widen(float f) {
@@ -602,8 +605,15 @@ __device__ __forceinline__ double widen(float f) {
 //   X_s = t1(a,i)u(b,c,j,k) - t1(a,j)u(b,c,i,k) + t1(a,k)u(b,c,i,j)
 //       - t1(b,i)u(a,c,j,k) + t1(b,j)u(a,c,i,k) - t1(b,k)u(a,c,i,j)
 //       + t1(c,i)u(a,b,j,k) - t1(c,j)u(a,b,i,k) + t1(c,k)u(a,b,i,j)   (FP32)
-//   D = (e_i + e_j + e_k) - (e_a + e_b + e_c)                          (FP64)
-//   e1 += X^2 / D,  est += X X_s / D                                    (FP64)
+//   D = (e_i + e_j + e_k) - (e_a + e_b + e_c)                          (FP32)
+//   q = X / D; per c, the four k terms q X and q X_s summed in FP32,
+//   then added to e1 and est                                            (FP64)
+// The orbital energies are FP32 copies of e - mu, mu the midpoint of the
+// gap between the highest occupied and the lowest virtual level: every
+// hole term of D is then negative and every particle term positive, so
+// |D| is the sum of the terms' magnitudes and the FP32 sums round to a few
+// units in the last place of |D| (relative ~1e-7), far below the error of
+// the split products.
 __device__ __forceinline__ float4 ld4(const float *p) { return __ldg(reinterpret_cast<const float4 *>(p)); }
 __device__ __forceinline__ float el(const float4 &x, int k) { return k == 0 ? x.x : k == 1 ? x.y : k == 2 ? x.z : x.w; }
 
@@ -620,13 +630,13 @@ __device__ __forceinline__ void energy_chunk(const float (&R)[N], const EDesc &d
     const int ga = d.g[0] + a, gb = d.g[1] + b, gi = d.g[3] + i, gj = d.g[4] + j;
     const int pi = d.gp[3] + i, pj = d.gp[4] + j, pk0 = d.gp[5];  // padded holes
     const int nc = d.nv[2], nk = d.nv[5], gc0 = d.g[2], gk0 = d.g[5];
-    const double *__restrict__ eo = d.eo;
-    const double *__restrict__ ev = d.ev;
-    const double eij = __ldg(eo + gi) + __ldg(eo + gj);
-    const double eab = __ldg(ev + ga) + __ldg(ev + gb);
-    double P[4];  // e_i + e_j + e_k
+    const float *__restrict__ eo = d.eo;
+    const float *__restrict__ ev = d.ev;
+    const float eij = __ldg(eo + gi) + __ldg(eo + gj);
+    const float eab = __ldg(ev + ga) + __ldg(ev + gb);
+    float P[4];  // e_i + e_j + e_k
 #pragma unroll
-    for (int k = 0; k < 4; ++k) P[k] = k < nk ? eij + __ldg(eo + gk0 + k) : 0.0;
+    for (int k = 0; k < 4; ++k) P[k] = k < nk ? eij + __ldg(eo + gk0 + k) : -1.0f;
     const float *__restrict__ t1a = d.T1f + (int64_t)ga * op;
     const float *__restrict__ t1b = d.T1f + (int64_t)gb * op;
     const float t1ai = __ldg(t1a + pi), t1aj = __ldg(t1a + pj), t1bi = __ldg(t1b + pi), t1bj = __ldg(t1b + pj);
@@ -646,7 +656,8 @@ __device__ __forceinline__ void energy_chunk(const float (&R)[N], const EDesc &d
             const float4 ubcj = ld4(ubc + pj * op + pk0), ubci = ld4(ubc + pi * op + pk0);
             const float4 uacj = ld4(uac + pj * op + pk0), uaci = ld4(uac + pi * op + pk0);
             const float4 t1ck = ld4(t1c + pk0);
-            const double Q = eab + __ldg(ev + gc);
+            const float Q = eab + __ldg(ev + gc);
+            float e1c = 0.0f, estc = 0.0f;
 #pragma unroll
             for (int k = 0; k < 4; ++k) {
                 if (k < nk) {
@@ -659,13 +670,14 @@ __device__ __forceinline__ void energy_chunk(const float (&R)[N], const EDesc &d
                     s = fmaf(t1ci, el(uabj, k), s);
                     s = fmaf(-t1cj, el(uabi, k), s);
                     s = fmaf(el(t1ck, k), uabij, s);
-                    const double x = widen(R[OFF + c * 4 + k]);
-                    const double D = P[k] - Q;
-                    const double q = div_nr(x, D);
-                    e1 = fma(q, x, e1);
-                    est = fma(q, widen(s), est);
+                    const float x = R[OFF + c * 4 + k];
+                    const float q = __fdividef(x, P[k] - Q);
+                    e1c = fmaf(q, x, e1c);
+                    estc = fmaf(q, s, estc);
                 }
             }
+            e1 += widen(e1c);
+            est += widen(estc);
         }
     }
 }
@@ -683,12 +695,12 @@ __device__ __forceinline__ void energy_tmem(uint32_t th, const EDesc &d, int par
     const int gb = d.g[1] + b, gi = d.g[3] + i, gj = d.g[4] + j;
     const int pi = d.gp[3] + i, pj = d.gp[4] + j, pk0 = d.gp[5];
     const int nc = d.nv[2], nk = d.nv[5], gc0 = d.g[2], gk0 = d.g[5];
-    const double *__restrict__ eo = d.eo;
-    const double *__restrict__ ev = d.ev;
-    double P[4];
-    const double eij = row_ok ? __ldg(eo + gi) + __ldg(eo + gj) : 0.0;
+    const float *__restrict__ eo = d.eo;
+    const float *__restrict__ ev = d.ev;
+    float P[4];
+    const float eij = row_ok ? __ldg(eo + gi) + __ldg(eo + gj) : 0.0f;
 #pragma unroll
-    for (int k = 0; k < 4; ++k) P[k] = (row_ok && k < nk) ? eij + __ldg(eo + gk0 + k) : 0.0;
+    for (int k = 0; k < 4; ++k) P[k] = (row_ok && k < nk) ? eij + __ldg(eo + gk0 + k) : -1.0f;
     const float *__restrict__ t1b = d.T1f + (int64_t)(row_ok ? gb : 0) * op;
     const float t1bi = row_ok ? __ldg(t1b + pi) : 0.f, t1bj = row_ok ? __ldg(t1b + pj) : 0.f;
     const float4 t1bk = row_ok ? ld4(t1b + pk0) : make_float4(0.f, 0.f, 0.f, 0.f);
@@ -701,7 +713,7 @@ __device__ __forceinline__ void energy_tmem(uint32_t th, const EDesc &d, int par
         const float *__restrict__ uab = d.Uf + ((int64_t)(ok_a ? ga : 0) * v + (ok_a ? gb : 0)) * oo;
         float t1ai = 0.f, t1aj = 0.f, uabij = 0.f;
         float4 t1ak = make_float4(0.f, 0.f, 0.f, 0.f), uabj = t1ak, uabi = t1ak;
-        double eab = 0.0;
+        float eab = 0.0f;
         if (ok_a) {
             t1ai = __ldg(t1a + pi);
             t1aj = __ldg(t1a + pj);
@@ -724,7 +736,8 @@ __device__ __forceinline__ void energy_tmem(uint32_t th, const EDesc &d, int par
             const float4 ubcj = ld4(ubc + pj * op + pk0), ubci = ld4(ubc + pi * op + pk0);
             const float4 uacj = ld4(uac + pj * op + pk0), uaci = ld4(uac + pi * op + pk0);
             const float4 t1ck = ld4(t1c + pk0);
-            const double Q = eab + __ldg(ev + gc);
+            const float Q = eab + __ldg(ev + gc);
+            float e1c = 0.0f, estc = 0.0f;
 #pragma unroll
             for (int k = 0; k < 4; ++k) {
                 if (k < nk) {
@@ -737,13 +750,14 @@ __device__ __forceinline__ void energy_tmem(uint32_t th, const EDesc &d, int par
                     s = fmaf(t1ci, el(uabj, k), s);
                     s = fmaf(-t1cj, el(uabi, k), s);
                     s = fmaf(el(t1ck, k), uabij, s);
-                    const double x = widen(el(x4, k));
-                    const double D = P[k] - Q;
-                    const double q = div_nr(x, D);
-                    e1 = fma(q, x, e1);
-                    est = fma(q, widen(s), est);
+                    const float x = el(x4, k);
+                    const float q = __fdividef(x, P[k] - Q);
+                    e1c = fmaf(q, x, e1c);
+                    estc = fmaf(q, s, estc);
                 }
             }
+            e1 += widen(e1c);
+            est += widen(estc);
         }
     }
 }
@@ -981,8 +995,8 @@ __device__ __forceinline__ void split_body(const SplitParams &gp, const QueueCtl
                         desc->op = p.op;
                         desc->T1f = p.T1f;
                         desc->Uf = p.Uf;
-                        desc->eo = p.evl;
-                        desc->ev = p.evl + p.nocc;
+                        desc->eo = p.evf;
+                        desc->ev = p.evf + p.nocc;
                         desc->part = p.part;
                         desc->inv_s = p.inv_s;
                         desc->inv_s2 = p.inv_s2;
@@ -1372,11 +1386,12 @@ int mixed_prepare(sdt_job *j, int type, cudaStream_t st) {
     }
     tr.mark("pack", st);
     // FP32 copies of T1 [v][OP] and the vvoo block [v][v][OP][OP] for the s1
-    // terms, holes padded per tile to multiples of 4.
+    // terms, holes padded per tile to multiples of 4; the T1 buffer also holds
+    // the shifted FP32 orbital energies after the T1 copy (o + v values).
     const int64_t OP = 4 * NOB;
     const int64_t n_t1 = v * OP, n_u = v * v * OP * OP;
     if (!rc) {
-        j->t1f = (float *)gpu_get(std::max<int64_t>(n_t1, 1) * sizeof(float));
+        j->t1f = (float *)gpu_get((n_t1 + o + v) * sizeof(float));
         j->uf = (float *)gpu_get(std::max<int64_t>(n_u, 1) * sizeof(float));
         if (!j->t1f || !j->uf) {
             mixed_release(j);
@@ -1390,6 +1405,19 @@ int mixed_prepare(sdt_job *j, int type, cudaStream_t st) {
                                                       t32 + 2 * o_on);
         count_launch();
         rc = cuda_check(cudaGetLastError(), "mixed form: split");
+    }
+    std::vector<float> evf(o + v);
+    if (!rc) {
+        // orbital energies minus the midpoint of the occupied-virtual gap: every
+        // hole term of a denominator is then negative and every particle term
+        // positive, so its FP32 sums do not cancel
+        double emax = -1e300, emin = 1e300;
+        for (int64_t x = 0; x < o; ++x) emax = std::max(emax, j->evl[x]);
+        for (int64_t x = o; x < o + v; ++x) emin = std::min(emin, j->evl[x]);
+        const double mu = (o > 0 && v > 0) ? 0.5 * (emax + emin) : 0.0;
+        for (int64_t x = 0; x < o + v; ++x) evf[x] = (float)(j->evl[x] - mu);
+        rc = cuda_check(cudaMemcpyAsync(j->t1f + n_t1, evf.data(), (o + v) * sizeof(float), cudaMemcpyHostToDevice, st),
+                        "mixed form: orbital energies");
     }
     if (!rc) rc = cuda_check(cudaStreamSynchronize(st), "mixed form: prepare");
     tr.mark("fp32 copies", nullptr);
@@ -1436,6 +1464,7 @@ SplitParams job_params(sdt_job *j, const LaunchArgs &a) {
     p.Uf = j->uf;
     p.op = 4 * j->nob;
     p.evl = j->evl_d;
+    p.evf = j->t1f + (int64_t)t.nvir * 4 * j->nob;
     p.tiles = j->tiles;
     p.noab = (int32_t)t.noab;
     p.nvab = (int32_t)t.nvab;
