@@ -69,25 +69,29 @@ constexpr int SX_EPI = 256;                   // energy threads (warps 8-15)
 // 128*56 + 128*72 + 512*88 = 61440 = 768*80, and per sub-partition
 // (56 + 72 + 4*88)*32 = 15360 <= 16384.
 constexpr int SX_THREADS_H = 768, SX_EPI_H = 512;
-constexpr int SX_REG_LAUNCH_H = 80, SX_REG_HIGH_H = 88;
+constexpr int SX_REG_LAUNCH_H = 80, SX_REG_HIGH_H = 88, SX_REG_DRAIN_H = 72;
 // Register split (setmaxnreg): the launch gives 128 per thread (4 warps per
-// SM sub-partition); warps 0-3 drop to 56, the drain warps to 72 and the
-// energy warps rise to 192: 128*56 + 128*72 + 256*192 = 65536 = 512*128, and
-// each sub-partition holds one warp of each group: (56+72+2*192)*32 = 16384.
-constexpr int SX_REG_LAUNCH = 128, SX_REG_LOW = 56, SX_REG_DRAIN = 72, SX_REG_HIGH = 192;
+// SM sub-partition); warps 0-3 drop to 56, the drain warps to 88 and the
+// energy warps rise to 176: 128*56 + 128*88 + 256*176 = 63488 <= 512*128,
+// and each sub-partition holds one warp of warps 0-3, one drain warp and two
+// energy warps: (56+88+2*176)*32 = 15872 <= 16384.  (Measured against 72 /
+// 192: the drains are the short-K bottleneck, the FP32 energy pass fits in
+// 176.)
+constexpr int SX_REG_LAUNCH = 128, SX_REG_LOW = 56, SX_REG_DRAIN = 88, SX_REG_HIGH = 176;
 static_assert(128 * SX_REG_LOW + 128 * SX_REG_DRAIN + 256 * SX_REG_HIGH <= SX_THREADS * SX_REG_LAUNCH,
               "register split");
+static_assert((SX_REG_LOW + SX_REG_DRAIN + 2 * SX_REG_HIGH) * 32 <= 16384, "register split: sub-partition registers");
 // setmaxnreg.dec may only lower and setmaxnreg.inc only raise a warp's count.
 static_assert(SX_REG_LOW <= SX_REG_LAUNCH && SX_REG_DRAIN <= SX_REG_LAUNCH && SX_REG_HIGH >= SX_REG_LAUNCH,
               "setmaxnreg direction");
 static_assert(SX_REG_LAUNCH_H * SX_THREADS_H <= 65536 && SX_REG_LAUNCH_H % 8 == 0 &&
                   (SX_REG_LAUNCH_H + 8) * SX_THREADS_H > 65536,
               "hold variant: launch registers = the most 768 threads can have");
-static_assert(128 * SX_REG_LOW + 128 * SX_REG_DRAIN + SX_EPI_H * SX_REG_HIGH_H <= SX_THREADS_H * SX_REG_LAUNCH_H,
+static_assert(128 * SX_REG_LOW + 128 * SX_REG_DRAIN_H + SX_EPI_H * SX_REG_HIGH_H <= SX_THREADS_H * SX_REG_LAUNCH_H,
               "hold variant: register split");
-static_assert(SX_REG_LOW <= SX_REG_LAUNCH_H && SX_REG_DRAIN <= SX_REG_LAUNCH_H && SX_REG_HIGH_H >= SX_REG_LAUNCH_H,
+static_assert(SX_REG_LOW <= SX_REG_LAUNCH_H && SX_REG_DRAIN_H <= SX_REG_LAUNCH_H && SX_REG_HIGH_H >= SX_REG_LAUNCH_H,
               "hold variant: setmaxnreg direction");
-static_assert((SX_REG_LOW + SX_REG_DRAIN + 4 * SX_REG_HIGH_H) * 32 <= 16384, "hold variant: sub-partition registers");
+static_assert((SX_REG_LOW + SX_REG_DRAIN_H + 4 * SX_REG_HIGH_H) * 32 <= 16384, "hold variant: sub-partition registers");
 constexpr int SX_BV = 8, SX_BO = 4, SX_NX = 32768;
 constexpr int SX_NS = 4;                      // operand stages
 constexpr int SX_A = 128 * 32, SX_B = 256 * 32;
@@ -873,7 +877,7 @@ __device__ __forceinline__ void split_body(const SplitParams &gp, const QueueCtl
             run_mma<TYPE, NB, QUEUE>(gp, q, stages, full, empty, tfull, tempty, drain, tmem, abort, ring);
     } else if (warp < 8) {
         // ---------------- drain warps ----------------
-        asm volatile("setmaxnreg.dec.sync.aligned.u32 %0;" ::"n"(SX_REG_DRAIN));
+        asm volatile("setmaxnreg.dec.sync.aligned.u32 %0;" ::"n"(HOLD ? SX_REG_DRAIN_H : SX_REG_DRAIN));
         const int quad = warp & 3;
         const int m = quad * 32 + lane;  // TMEM lane = GEMM row
         const bool leader = (warp == 4 && lane == 0);
