@@ -25,10 +25,12 @@
 // uses a swizzled hole index so that the rows a warp drains fall in distinct
 // shared-memory banks for all 9 layouts.
 //
-// Energies.  When an item's last term is drained, the energy warps copy the
-// finished sub-box from shared memory into registers (128 values per thread)
-// and release it; the drain warps then store the next item's first term into
-// it while the energy warps evaluate the copy: the s1 products in FP32 from
+// Energies.  When an item's eighth term is drained, the energy warps copy
+// the sub-box from shared memory into registers (128 values per thread), add
+// the ninth term's accumulator from TMEM to it themselves (its rows (b;i,j)
+// and columns (a,c;k) are the layout of their copy), and release both; the
+// drain warps then store the next item's first term into the sub-box while
+// the energy warps evaluate the copy: the s1 products in FP32 from
 // FP32 copies of T1 and the vvoo block, the denominator and the quotient in
 // FP32 (orbital energies shifted by the midpoint of the occupied-virtual
 // gap, so that no sum in a denominator cancels), and the two energy sums in
@@ -72,12 +74,11 @@ constexpr int SX_THREADS_H = 768, SX_EPI_H = 512;
 constexpr int SX_REG_LAUNCH_H = 80, SX_REG_HIGH_H = 88, SX_REG_DRAIN_H = 72;
 // Register split (setmaxnreg): the launch gives 128 per thread (4 warps per
 // SM sub-partition); warps 0-3 drop to 56, the drain warps to 88 and the
-// energy warps rise to 176: 128*56 + 128*88 + 256*176 = 63488 <= 512*128,
+// energy warps rise to 184: 128*56 + 128*88 + 256*184 = 65536 = 512*128,
 // and each sub-partition holds one warp of warps 0-3, one drain warp and two
-// energy warps: (56+88+2*176)*32 = 15872 <= 16384.  (Measured against 72 /
-// 192: the drains are the short-K bottleneck, the FP32 energy pass fits in
-// 176.)
-constexpr int SX_REG_LAUNCH = 128, SX_REG_LOW = 56, SX_REG_DRAIN = 88, SX_REG_HIGH = 176;
+// energy warps: (56+88+2*184)*32 = 16384.  (Measured against 72 / 192: the
+// drains are the short-K bottleneck, and the FP32 energy pass fits in 184.)
+constexpr int SX_REG_LAUNCH = 128, SX_REG_LOW = 56, SX_REG_DRAIN = 88, SX_REG_HIGH = 184;
 static_assert(128 * SX_REG_LOW + 128 * SX_REG_DRAIN + 256 * SX_REG_HIGH <= SX_THREADS * SX_REG_LAUNCH,
               "register split");
 static_assert((SX_REG_LOW + SX_REG_DRAIN + 2 * SX_REG_HIGH) * 32 <= 16384, "register split: sub-partition registers");
@@ -835,6 +836,8 @@ __device__ __forceinline__ void split_body(const SplitParams &gp, const QueueCtl
     volatile int64_t *en_unit = (volatile int64_t *)(misc + 216);
     int *dr_nk = (int *)(misc + 224);              // [9] kept K chunks per term of the drained item
     volatile int *dr_kseg = (volatile int *)(misc + 264);  // K chunks per drain of the drained item's job
+    volatile int *en_buf = (volatile int *)(misc + 268);   // register hold: accumulator of the last term's
+    volatile int *en_add = (volatile int *)(misc + 272);   // last segment, and whether it holds a product
     int *errp = QUEUE ? q.err : gp.err;
     EDesc *desc = (EDesc *)(misc + 320);
     double *red = (double *)(misc + 512);          // [16 energy warps at most][2]
@@ -912,6 +915,13 @@ __device__ __forceinline__ void split_body(const SplitParams &gp, const QueueCtl
                     const int buf = sg % NB;
                     const bool first = (t == 0 && sgi == 0);
                     const bool last = (t == 8 && sgi == nseg - 1);
+                    if (!HOLD && last) {
+                        // register hold: the energy warps add the last segment to their copy
+                        // of the sub-box themselves (its rows and columns are theirs), so
+                        // the sub-box is ready once the segments before it are drained
+                        if (leader) tc::mbar_arrive(xready);
+                        continue;
+                    }
                     if (leader) {
                         bool w = tc::mbar_wait(&tfull[buf], (sg / NB) & 1, kWaitNs, abort);
                         // registers hold: the previous item's values must have left the sub-box;
@@ -972,6 +982,7 @@ __device__ __forceinline__ void split_body(const SplitParams &gp, const QueueCtl
         const int quarter0 = HOLD ? half : 2 * half;
         int slot = 0;            // queue mode, leader: the current item's job slot and item count
         int64_t job_items = 0;
+        uint32_t en_sg = 0;      // register hold, leader: accumulator segments of the items so far
         for (int n = 0;; ++n) {
             if (leader) {
                 int64_t si = ring_take(ring, n, abort);
@@ -1005,6 +1016,23 @@ __device__ __forceinline__ void split_body(const SplitParams &gp, const QueueCtl
                         desc->inv_s = p.inv_s;
                         desc->inv_s2 = p.inv_s2;
                         desc->nvir = p.nvir;
+                        if constexpr (!HOLD) {
+                            // the item's segments in the MMA's order; the last one (term 8)
+                            // is added here, not by the drains
+                            uint32_t nsg = 0;
+                            int nk8 = 0;
+                            for (int t = 0; t < 9; ++t) {
+                                const int nk = term_chunk_count<KE>(p, bx, t);
+                                int kseg;
+                                nsg += (uint32_t)term_segments(nk, p.kseg, kseg);
+                                if (t == 8) nk8 = nk;
+                            }
+                            const uint32_t sgl = en_sg + nsg - 1;
+                            en_sg += nsg;
+                            w = tc::mbar_wait(&tfull[sgl % NB], (sgl / NB) & 1, kWaitNs, abort);
+                            *en_buf = (int)(sgl % NB);
+                            *en_add = nk8 > 0 ? 1 : 0;
+                        }
                     }
                 }
                 if (!w) {
@@ -1034,8 +1062,25 @@ __device__ __forceinline__ void split_body(const SplitParams &gp, const QueueCtl
                     for (int c = 0; c < 8; ++c)
 #pragma unroll
                         for (int k = 0; k < 4; ++k) R[A * 32 + c * 4 + k] = X[xaddr(4 * half + A, rb, c, ri, rj_, k)];
+                // the last term (rows (b;i,j), columns (a,c;k), sign +1): this thread's row,
+                // columns 128*half .. +127 of the accumulator
+                tc::tc_fence_after();
+                if (*en_add) {
+                    const uint32_t ta = tmem + ((uint32_t)((warp & 3) * 32) << 16) + (uint32_t)(*en_buf * 256 + 128 * half);
+#pragma unroll
+                    for (int h = 0; h < 8; ++h) {
+                        float v[16];
+                        tc::tmem_ld16(ta + (uint32_t)(16 * h), v);
+#pragma unroll
+                        for (int q = 0; q < 16; ++q) R[16 * h + q] += v[q];
+                    }
+                }
+                tc::tc_fence_before();
                 named_bar(2, EPI);
-                if (leader) tc::mbar_arrive(xfree);
+                if (leader) {
+                    tc::mbar_arrive(&tempty[*en_buf]);
+                    tc::mbar_arrive(xfree);
+                }
                 if (d.item >= 0) {  // a box outside the tuple has no item
                     energy_chunk<0, 0, 128>(R, d, half, rb, ri, rj_, e1[0], est[0]);
                     energy_chunk<1, 32, 128>(R, d, half, rb, ri, rj_, e1[0], est[0]);
