@@ -383,9 +383,10 @@ int sdt_tc_selftest(const float *a_hi, const float *a_lo, const float *b_hi,
  * values in device arrays, K a multiple of 8), kind::f16 MMAs. */
 int sdt_tc_selftest16(const void *a_hi, const void *a_lo, const void *b_hi,
                       const void *b_lo, int K, int bf16, float *D);
-/* Check of the FP64 division of the mixed form's energy epilogue (no
- * reference counterpart): largest relative difference from the IEEE
- * quotient over n seeded (numerator, denominator) pairs. */
+/* Check of the mixed form's FP32 energy quotient (no reference
+ * counterpart): largest relative difference of X/D, with D summed in FP32
+ * from gap-shifted orbital energies the way the energy epilogue sums it,
+ * from the FP64 quotient, over n seeded samples. */
 int sdt_check_division(int64_t n, uint64_t seed, double *max_rel_err);
 /* Failure-path check (no reference counterpart): one bounded device wait on
  * an mbarrier nothing arrives on, limited to timeout_s (0 < timeout_s <= 1).

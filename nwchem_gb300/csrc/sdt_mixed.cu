@@ -247,21 +247,48 @@ int run_selftest(const void *a_hi, const void *a_lo, const void *b_hi, const voi
     return SDT_OK;
 }
 
-// Maximum relative error of div_nr against the IEEE quotient over n pairs:
-// x ~ U(-1,1) * 2^e (e in [-40, 40)), D in the range of (T) denominators
-// ([-12, -0.5]) and a wider one ([-1e3, -1e-3]).
+// Maximum relative error of the mixed form's FP32 energy quotient X/D
+// against FP64 over n seeded samples, computed the way the energy warps
+// compute it: orbital energies rounded to FP32 after the shift by the gap
+// midpoint mu, D = ((e_i + e_j) + e_k) - ((e_a + e_b) + e_c) in FP32, and
+// q = __fdividef(x, D).  Occupied levels in [-20, -0.25] (one sample in four
+// with every hole in the valence range [-1.5, -0.25]), virtual levels in
+// [0.05, 8], so mu = -0.1; x ~ U(-1,1) * 2^e (e in [-40, 40)), an FP32
+// value.  The reference is x / D with D summed in FP64 from the unshifted
+// levels.
 __global__ void division_check_kernel(int64_t n, uint64_t seed, unsigned long long *worst_bits) {
+    constexpr double kMu = -0.1;
     double worst = 0.0;
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         uint64_t z = seed + 0x9E3779B97F4A7C15ull * (uint64_t)(i + 1);
-        z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
-        z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
-        z ^= z >> 31;
-        const double u1 = (double)(z >> 11) * 0x1.0p-53, u2 = (double)((z * 0x2545F4914F6CDD1Dull) >> 11) * 0x1.0p-53;
-        const int e = (int)((z >> 3) % 80) - 40;
-        const double x = ldexp(2.0 * u1 - 1.0, e);
-        const double D = (i & 1) ? -(0.5 + 11.5 * u2) : -exp2(-10.0 + 20.0 * u2);
-        const double q = div_nr(x, D), ref = x / D;
+        double u[8];
+#pragma unroll
+        for (int r = 0; r < 8; ++r) {
+            z += 0x9E3779B97F4A7C15ull;
+            uint64_t y = z;
+            y = (y ^ (y >> 30)) * 0xBF58476D1CE4E5B9ull;
+            y = (y ^ (y >> 27)) * 0x94D049BB133111EBull;
+            y ^= y >> 31;
+            u[r] = (double)(y >> 11) * 0x1.0p-53;
+        }
+        const bool valence = (i & 3) == 0;
+        double eo[3], ev[3];
+#pragma unroll
+        for (int r = 0; r < 3; ++r) {
+            eo[r] = valence ? -(0.25 + 1.25 * u[r]) : -(0.25 + 19.75 * u[r]);
+            ev[r] = 0.05 + 7.95 * u[3 + r];
+        }
+        const int e = (int)(u[6] * 80.0) - 40;
+        const float x = (float)ldexp(2.0 * u[7] - 1.0, e);
+        float fo[3], fv[3];
+#pragma unroll
+        for (int r = 0; r < 3; ++r) {
+            fo[r] = (float)(eo[r] - kMu);
+            fv[r] = (float)(ev[r] - kMu);
+        }
+        const float D32 = ((fo[0] + fo[1]) + fo[2]) - ((fv[0] + fv[1]) + fv[2]);
+        const double D64 = (eo[0] + eo[1] + eo[2]) - (ev[0] + ev[1] + ev[2]);
+        const double q = (double)__fdividef(x, D32), ref = (double)x / D64;
         if (ref != 0.0) worst = fmax(worst, fabs(q - ref) / fabs(ref));
     }
     atomicMax(worst_bits, (unsigned long long)__double_as_longlong(worst));

@@ -225,16 +225,4 @@ __device__ __forceinline__ float to_tf32(float x) {
 
 }  // namespace tc
 
-// x / D in FP64 without the IEEE division sequence: the hardware reciprocal
-// approximation (PTX rcp.approx.ftz.f64) refined by one Newton-Raphson step
-// r' = r + r(1 - D r), which squares its relative error, then the product
-// x * r'.  Not correctly rounded; the relative error bound is checked on the
-// device by sdt_check_division.  Intended for normal, non-zero D.
-__device__ __forceinline__ double div_nr(double x, double D) {
-    double r;
-    asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(r) : "d"(D));
-    const double e = fma(-D, r, 1.0);
-    r = fma(r, e, r);
-    return x * r;
-}
 }  // namespace sdt

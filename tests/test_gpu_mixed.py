@@ -79,12 +79,15 @@ def test_tcgen05_split_gemm16(cuda_device, bf16, K):
 
 
 def test_energy_division_bound(cuda_device):
-    """The epilogue's FP64 division (reciprocal approximation + one
-    Newton-Raphson step) stays within 1e-11 of the IEEE quotient."""
+    """The epilogue's FP32 quotient X/D -- orbital energies shifted by the
+    gap midpoint and rounded to FP32, D summed in FP32 (every hole term
+    negative, every particle term positive, so no sum cancels), then
+    __fdividef -- stays within 1e-6 of the FP64 quotient: at most ten FP32
+    roundings relative to |D| (6e-7) plus 2 ulp for the division (1.2e-7)."""
     lib = _capi.lib()
     err = C.c_double()
     _capi.check(lib.sdt_check_division(1 << 22, 12345, C.byref(err)), "sdt_check_division")
-    assert 0.0 <= err.value < 1e-11, err.value
+    assert 0.0 < err.value < 1e-6, err.value
 
 
 MIXED_TILINGS = [
