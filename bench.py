@@ -27,7 +27,9 @@ The default run also reports (--extras): the mixed forms on the same steps
 with absolute errors; the o=64/v=512 workload (FP64 on one seeded tuple,
 each mixed form on 48 tuples, segmented drains); a molecular-magnitude case
 (the o=40/v=300 inputs scaled so one step's |E(T)| is 0.05 Eh); and a
-serving stream through the shared work queue.
+serving stream through the shared work queue.  On one GB300 the default
+run takes about ten minutes: the 20 timed FP64 steps ~85 s, the o=64/v=512
+FP64 tuple ~82 s, the serving stream's two deferred FP64 checks ~2 min.
 Multi-GPU: each rank takes its own slices (weak scaling, no collective on
 the data path); energies are summed on the host.
 """
