@@ -831,7 +831,6 @@ __device__ __forceinline__ void split_body(const SplitParams &gp, const QueueCtl
     uint32_t *tslot = (uint32_t *)(misc + 192);
     volatile int *abort = (volatile int *)(misc + 196);
     volatile int *dr_ok = (volatile int *)(misc + 200);
-    volatile int *en_ok = (volatile int *)(misc + 204);
     volatile int64_t *dr_unit = (volatile int64_t *)(misc + 208);
     volatile int64_t *en_unit = (volatile int64_t *)(misc + 216);
     int *dr_nk = (int *)(misc + 224);              // [9] kept K chunks per term of the drained item
@@ -863,7 +862,6 @@ __device__ __forceinline__ void split_body(const SplitParams &gp, const QueueCtl
         }
         *abort = 0;
         *dr_ok = 1;
-        *en_ok = 1;
         tc::fence_mbar_init();
     }
     if (warp == 1) tc::tmem_alloc(tslot, 512);
