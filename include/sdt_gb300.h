@@ -220,7 +220,8 @@ int sdt_job_run(sdt_job *job, const int64_t *klist, int64_t n,
                 int precision, double *energy, double *per_task,
                 void *stream);
 int sdt_job_destroy(sdt_job *job);
-/* Device bytes held by a job. */
+/* Device bytes held by a job: its dense FP64 operands and, once a mixed
+ * precision has run, that form's split operands, FP32 copies and tables. */
 int64_t sdt_job_device_bytes(const sdt_job *job);
 /* Mixed form: drain the tensor-core accumulator every `chunks` K chunks
  * (8 TF32 or 16 BF16/FP16 values each; 0, the default: once per

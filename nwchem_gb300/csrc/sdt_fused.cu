@@ -544,7 +544,8 @@ extern "C" int64_t sdt_job_device_bytes(const sdt_job *j) {
     if (!j) return 0;
     int64_t b = 0;
     for (int a = 0; a < DST_N; ++a) b += (int64_t)j->arr_n[a] * 8;
-    return b;
+    for (int k = 0; k < 2 * SP_N; ++k) b += (int64_t)j->sp_n[k];
+    return b + (int64_t)j->mixed_aux_n;
 }
 
 // One read per host page of a buffer, just before the copy engines read it.

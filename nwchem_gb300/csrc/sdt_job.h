@@ -38,6 +38,7 @@ struct sdt_job {
     size_t sp_n[2 * sdt::SP_N] = {0};    // bytes
     int mixed_type = -1;                 // TM_* of the prepared copies, -1: none
     float *t1f = nullptr, *uf = nullptr;
+    size_t mixed_aux_n = 0;              // bytes of the FP32 copies and the box tables
     double inv_s = 1.0, inv_s2 = 1.0;    // FP16: 1/(s_T s_I), its square
     int64_t *tile_box_d = nullptr;       // device table buffer (box tables, pair blocks)
     int64_t tile_box_off = 0, pair_blk_off = 0;

@@ -109,7 +109,10 @@ int64_t job_bytes(const sdt_tiling *ti, int precision) {
         const int64_t blocks_a = nvb * nob * nob * (nko + nkv);
         const int64_t blocks_b = nvb * nvb * nob * nko + vd2_blocks_pairs * nob * nkv;
         bytes += 2 * (blocks_a * 4096 + blocks_b * 8192);
-        bytes += 4 * (v * o + v * v * o * o);
+        // FP32 copies of T1 and the vvoo block with holes padded per tile to
+        // multiples of 4, then the orbital energies
+        const int64_t op = 4 * nob;
+        bytes += 4 * (v * op + v * v * op * op + o + v);
     }
     return bytes + bytes / 20 + (64ll << 20);
 }

@@ -1281,6 +1281,7 @@ void mixed_release(sdt_job *j) {
     gpu_put(j->tile_box_d);
     j->t1f = j->uf = nullptr;
     j->tile_box_d = nullptr;
+    j->mixed_aux_n = 0;
     j->mixed_type = -1;
 }
 
@@ -1383,6 +1384,7 @@ int mixed_prepare(sdt_job *j, int type, cudaStream_t st) {
         return fail(SDT_ERR_NOMEM, "mixed form: tables");
     }
     j->tile_box_d = tab_d;  // owns the whole table buffer
+    j->mixed_aux_n = std::max<size_t>(tab.size(), 1) * sizeof(int64_t);
     rc = cuda_check(cudaMemcpyAsync(tab_d, tab.data(), tab.size() * sizeof(int64_t), cudaMemcpyHostToDevice, st),
                     "mixed form: tables");
     j->tile_box_off = (int64_t)o_tbox;
@@ -1440,6 +1442,7 @@ int mixed_prepare(sdt_job *j, int type, cudaStream_t st) {
     if (!rc) {
         j->t1f = (float *)gpu_get((n_t1 + o + v) * sizeof(float));
         j->uf = (float *)gpu_get(std::max<int64_t>(n_u, 1) * sizeof(float));
+        j->mixed_aux_n += (size_t)(n_t1 + o + v + std::max<int64_t>(n_u, 1)) * sizeof(float);
         if (!j->t1f || !j->uf) {
             mixed_release(j);
             return fail(SDT_ERR_NOMEM, "mixed form: FP32 copies");

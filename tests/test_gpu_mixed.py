@@ -180,3 +180,22 @@ def test_mixed_work_unit_shapes(cuda_device, form):
     assert a[0] == b[0] and a[1] == b[1] and np.array_equal(a[2], b[2])
     bnd = MIXED_BOUND[form]
     assert b[0] == pytest.approx(f[0], rel=bnd) and b[1] == pytest.approx(f[1], rel=bnd)
+
+
+def test_job_bytes_bound_holds_for_padded_holes(cuda_device):
+    """The serving admission bound (sdt_job_bytes) covers what a job holds
+    after a mixed run, for occupied tiles of 5 (the FP32 s1 copies pad the
+    holes of each tile to a multiple of 4, 8 per tile here: 2.6x the dense
+    vvoo block)."""
+    import nwchem_gb300 as ng
+    from nwchem_gb300 import serve
+    t = ng.Tiling([5] * 8, [25] * 4).with_evl(5)
+    files = ng.synth_inputs(t, 5)
+    kl = ng.task_list(t)
+    with ng.TriplesJob(t) as job:
+        job.load(*files)
+        f64 = job.device_bytes
+        job.run(kl[:1], precision=PREC["fp16"])
+        mixed = job.device_bytes
+    assert 0 < f64 <= serve.job_bytes(t, ng.PREC_FP64)
+    assert f64 < mixed <= serve.job_bytes(t, ng.PREC_MIXED_FP16)
