@@ -307,7 +307,7 @@ int sdt_server_status(sdt_server *server, int64_t ticket, int *state,
  * quarter of the SMs without the queue. */
 int sdt_server_set_check_ctas(sdt_server *server, int ctas);
 /* The shared queue: its precision (SDT_PREC_FP64 turns it off), work-unit
- * shape (1 or 2, as sdt_job_set_mixed_shape; default 2), SMs kept free of
+ * shape (1 or 2, as sdt_job_set_mixed_shape; default 1), SMs kept free of
  * the resident kernel (default 16) and the seconds (at most 1) the kernel
  * waits for new work before it leaves (default 0.2).  Before the first
  * submit. */

@@ -145,7 +145,7 @@ struct sdt_server {
     };
     // The shared item queue (continuous batching), set up at its first use.
     struct Queue {
-        int precision = SDT_PREC_MIXED_FP16, type = TM_F16, shape = 2, reserve = 16, max_jobs = 4096;
+        int precision = SDT_PREC_MIXED_FP16, type = TM_F16, shape = 1, reserve = 16, max_jobs = 4096;
         double idle_s = 0.2;
         bool ready = false;
         size_t entry = 0;
@@ -186,22 +186,6 @@ struct sdt_server {
 
 namespace {
 
-// Work-unit shape for a job: the tensor-memory hold (2) when the contraction
-// length a sub-box sees is short -- (o + v) over the number of distinct
-// irreps below 320, where the FP64 energy work per element outweighs the
-// tensor-core work -- else the register hold (1).
-int mixed_shape(const sdt_tiling *t) {
-    int64_t o = 0, v = 0;
-    bool seen[8] = {false};
-    int nsym = 0;
-    for (int64_t b = 0; b < t->noab + t->nvab; ++b) {
-        (b < t->noab ? o : v) += t->range[b];
-        const int y = (int)(t->sym[b] & 7);
-        if (!seen[y]) seen[y] = true, ++nsym;
-    }
-    return (o + v) / std::max(nsym, 1) < 320 ? 2 : 1;
-}
-
 void run_one(sdt_server *s, sdt_server::Job *job) {
     cudaSetDevice(s->device);
     sdt_job *j = nullptr;
@@ -217,7 +201,6 @@ void run_one(sdt_server *s, sdt_server::Job *job) {
         failed(rc);
         return;
     }
-    if (job->precision != SDT_PREC_FP64) sdt_job_set_mixed_shape(j, mixed_shape(&job->t));
     rc = sdt_job_load(j, &job->f1, &job->f2, &job->fv, nullptr);
     job->t_loaded = s->now();
     int64_t n = 0;

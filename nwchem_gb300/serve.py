@@ -106,7 +106,7 @@ class Server:
     of waiting for work before the kernel leaves."""
 
     def __init__(self, budget_bytes: int, slots: int = 4, max_ctas: int = 0, check_ctas: int | None = None,
-                 queue: int | None = PREC_MIXED_FP16, shape: int = 2, reserve: int = 16, idle: float = 0.2):
+                 queue: int | None = PREC_MIXED_FP16, shape: int = 1, reserve: int = 16, idle: float = 0.2):
         self._lib = _capi.lib()
         h = C.c_void_p()
         _capi.check(self._lib.sdt_server_create(int(budget_bytes), int(slots), int(max_ctas), C.byref(h)),
