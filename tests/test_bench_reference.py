@@ -57,3 +57,12 @@ def test_reference_sample_is_uniform_over_the_slice():
     picks = np.concatenate([bench.ref_sample(sl, s) for s in range(200)])
     assert set(picks.tolist()) <= set(sl.tolist()) and len(set(picks.tolist())) == len(sl)
     assert np.array_equal(bench.ref_sample(sl, 7), bench.ref_sample(sl, 7))
+
+
+def test_reference_arm_other_ranks_exit_quietly():
+    """Under torchrun with N > 1 only rank 0 runs the reference arm and
+    prints its line; the other ranks exit 0 without work or output."""
+    r = _bench("--impl", "reference", "--gpus", "2", "--steps", "1", "--warmup", "3",
+               env_extra={"WORLD_SIZE": "2", "RANK": "1", "LOCAL_RANK": "1"}, timeout=120)
+    assert r.returncode == 0, r.stderr[-2000:]
+    assert not [ln for ln in r.stdout.splitlines() if ln.startswith("{")]
