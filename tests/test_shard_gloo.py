@@ -53,7 +53,7 @@ def _worker(rank, world, port, out, fail_rank):
 
 
 def _run(world, fail_rank=-1):
-    mgr = mp.Manager()
+    mgr = mp.get_context("spawn").Manager()   # no fork of this (threaded) process
     out = mgr.dict()
     mp.spawn(_worker, args=(world, _free_port(), out, fail_rank), nprocs=world, join=True)
     return dict(out)
